@@ -1,0 +1,140 @@
+/*
+ * movfem_gpu.h -- C-ABI of the GB300 edge-element assembly and complex sparse solve
+ * for MoVFEM_3DMT.
+ *
+ * The reference is a Fortran program whose hot path is three call sites in its
+ * frequency loop (MoVFEM_3DMT/src/MoVFEM_3DMT.f90):
+ *   :82   call global_vfem(mumps_par%irn, mumps_par%jcn, mumps_par%a, mumps_par%rhs)
+ *   :115  call zmumps(mumps_par)              ! job=6: analyse + factor + solve, nrhs=2
+ *   :123  call node_solution(mumps_par%rhs)   ! then receiver Z / rho / phi
+ * with the numbering built once by ga_init (global_assembly.f90:26-41).  The entry
+ * points below replace them; a Fortran host binds them with ISO_C_BINDING (see
+ * INTEGRATION.md).  Plain pointers and sizes only; every function returns 0 on
+ * success or a negative MVF_E_* code, and mvf_last_error() gives the message.
+ * The library never calls back into the host, and one context is used by one host
+ * thread at a time (the reference is single-threaded with module-level state).
+ *
+ * Conventions (as the reference): node id = (i*nny + j)*nnz + k; element id =
+ * (ie*ny + je)*nz + ke; symmetric tensors packed (xx, xy, xz, yy, yz, zz);
+ * complex numbers are interleaved (re, im) doubles; DOF numbers are 1-based, negative
+ * values are Dirichlet face flags (-1..-6 for x-, y-, z-, x+, y+, z+).
+ */
+#ifndef MOVFEM_GPU_H
+#define MOVFEM_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MVF_OK = 0,
+    MVF_E_ARG = -1,        /* invalid argument / size */
+    MVF_E_CUDA = -2,       /* a CUDA call failed */
+    MVF_E_SINGULAR = -3,   /* zero Jacobian or singular material tensor (n_fem.f90:374-377, problem.f90:260-271) */
+    MVF_E_NOCONV = -4,     /* solver stopped at its iteration cap above tolerance */
+    MVF_E_STATE = -5,      /* call out of order (e.g. solve before assemble) */
+    MVF_E_RECEIVER = -6,   /* receiver outside the inner grid (receiver_data.f90:187-209) */
+    MVF_E_NOMEM = -7,      /* device allocation failed */
+    MVF_E_UNSUPPORTED = -8 /* option not built */
+};
+
+/* Quirk switches; MVF_Q_ALL reproduces the reference. */
+#define MVF_Q_LIN_DZETA  1  /* n_fem.f90:193 linear dN/dzeta written with (1+nr1) */
+#define MVF_Q_FP32_CONST 2  /* default-real literals and kind-less cmplx() rounded to FP32 */
+#define MVF_Q_GPML_LAG   4  /* MoVFEM_3DMT.f90:203-206 GPML stretch uses the previous element's zone flags */
+#define MVF_Q_ALL        7
+
+/* Mesh and model: the arrays geometry.f90:17-24 holds after grid_3d, plus the
+ * boundary settings of PARAM.INP (MoVFEM_3DMT.f90:303-336).  Host pointers; copied. */
+typedef struct mvf_mesh {
+    int32_t nodes_per_elem;   /* 8, 20 or 27 (in_mn) */
+    int32_t nx, ny, nz;       /* elements per axis (g_nx-1, g_ny-1, g_nz-1) */
+    const double *xp;         /* [nnx] g_xp */
+    const double *yp;         /* [nny] g_yp */
+    const double *zp;         /* [npt] g_zp */
+    const double *sigma;      /* [npt][6] complex: g_sigma(6,g_npt) */
+    const double *mu;         /* [npt][6]: g_mu(6,g_npt) */
+    int32_t dirichlet;        /* PARAM.INP boundary: 1 Dirichlet, 0 GPML */
+    int32_t inimod;           /* Dirichlet primary model; 1 (zero secondary field) is built */
+    int32_t gpml_sch;         /* 0 Fang, 1 Zhou */
+    double a0, b0, nn;        /* GPML parameters */
+    int32_t nextd;            /* extension cells per side */
+    int32_t nzl_top;          /* g_nzl(g_nsf) */
+    int32_t nzl_air;          /* g_nzl(g_nsf-1) */
+    double ztop;              /* g_ztop */
+    int32_t quirks;           /* MVF_Q_* */
+} mvf_mesh;
+
+typedef struct mvf_stats {
+    int32_t outer_iters;      /* FP64 refinement steps */
+    int32_t inner_iters;      /* Krylov iterations (max over right-hand sides) */
+    double rel_residual;      /* max over RHS of ||b - A x|| / ||b|| in FP64 */
+    double seconds;           /* device time of the solve */
+    int64_t bytes_moved;      /* algorithmic HBM bytes of the executed kernels */
+} mvf_stats;
+
+typedef struct mvf_ctx mvf_ctx;
+
+/* Set-up (ga_init + init_* of MoVFEM_3DMT.f90:267-406): copies the model to the
+ * device, numbers the DOFs (global_assembly.f90:183-475), builds the CSR pattern
+ * (both triangles) and the discrete gradient used by the preconditioner.
+ * device < 0 keeps the current device. */
+int mvf_create(mvf_ctx **ctx, const mvf_mesh *mesh, int32_t device);
+void mvf_destroy(mvf_ctx *ctx);
+const char *mvf_last_error(const mvf_ctx *ctx);
+
+/* Sizes: free DOFs nne (global_assembly.f90:194), nnz of the full pattern, nnz of its
+ * lower triangle (the reference's nnze minus its never-written upper slots). */
+int mvf_sizes(const mvf_ctx *ctx, int32_t *nne, int64_t *nnz_full, int64_t *nnz_lower, int32_t *edges_per_elem,
+              int64_t *num_elems);
+
+/* Global DOF numbering gne(ne, me) in the reference's column-major layout
+ * (gne[im*ne + e]), bit-exact with c_gne12/36/54. */
+int mvf_numbering(const mvf_ctx *ctx, int32_t *gne);
+
+/* Replace the nodal conductivity (update_sigma, geometry.f90:144-153, runs on the host
+ * side of the boundary); [npt][6] complex. */
+int mvf_set_sigma(mvf_ctx *ctx, const double *sigma);
+
+/* Assembly for nfreq angular frequencies (global_vfem / local_vfem,
+ * MoVFEM_3DMT.f90:167-263): element curl-curl K_e, mass M_e and source b_e on the GPU,
+ * scattered into the CSR.  sigma_f: optional [nfreq][npt][6] complex per-frequency
+ * conductivity (NULL: the current one for all).  ifreq0: position of omega[0] in the
+ * reference's frequency loop (for the GPML zone-flag lag). */
+int mvf_assemble(mvf_ctx *ctx, int32_t nfreq, const double *omega, const double *sigma_f, int32_t ifreq0);
+
+/* Parity hook: the lower-triangle COO of frequency f that global_vfem would hand to
+ * MUMPS (before ga_sort_sparse, exact zeros kept), 1-based, in row-major order.
+ * ia/ja/a may be NULL to query *nnz.  a is complex. */
+int mvf_export_coo(const mvf_ctx *ctx, int32_t f, int32_t *ia, int32_t *ja, double *a, int64_t *nnz);
+/* Right-hand sides of frequency f: [2][nne] complex (mumps_par%rhs layout). */
+int mvf_export_rhs(const mvf_ctx *ctx, int32_t f, double *rhs);
+
+/* Parity hook: element matrices of elements [e0, e0+count) at frequency f of the last
+ * assembly: K, M [count][me][me] (real), b [count][me][2] complex. */
+int mvf_element_matrices(const mvf_ctx *ctx, int64_t e0, int64_t count, int32_t f, double *K, double *M,
+                         double *b);
+
+/* Solve (replaces zmumps job=6, MoVFEM_3DMT.f90:113-115): for every assembled
+ * frequency and both polarisations.  rhs_inout: [nfreq][2][nne] complex; on entry
+ * the right-hand sides (NULL: use the assembled ones), on exit the solutions (the
+ * mumps_par%rhs convention).  mode: 0 = mixed (complex FP32 FGMRES inside FP64
+ * iterative refinement, all frequencies batched), 1 = plain FP64 FGMRES one
+ * right-hand side at a time.  tol: FP64 relative residual target. */
+int mvf_solve(mvf_ctx *ctx, double *rhs_inout, double tol, int32_t mode, int32_t max_iters, mvf_stats *st);
+
+/* FP64 receiver evaluation (get_er / get_hr / interpolate_rx / get_impedance /
+ * get_res_phase: solution.f90:207-505, receiver_data.f90:111-253) on the last
+ * solution: Z [nfreq][nrx][4] complex, rho/phi [nfreq][nrx][4]; E, H optional
+ * [nfreq][nrx][2][3] complex. */
+int mvf_impedance(mvf_ctx *ctx, int32_t nrx, const double *xr, const double *yr, double *Z, double *rho,
+                  double *phi, double *E, double *H);
+
+/* Parity hook: y = A_f x for frequency f in FP64 (x, y: [2][nne] complex, host). */
+int mvf_spmv(mvf_ctx *ctx, int32_t f, const double *x, double *y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,219 @@
+"""Host-side mirror of the reference's hot-path call sites over the C-ABI.
+
+The reference's Fortran driver (MoVFEM_3DMT/src/MoVFEM_3DMT.f90) calls, per frequency,
+``global_vfem`` (:82) to assemble, ``zmumps`` with job=6 (:113-115) to solve both
+polarisations, and ``node_solution`` + ``write_receiver_data`` (:123-127) for E, H, Z,
+rho and phi.  :class:`MTProblem` exposes the same steps on the GPU library
+(``include/movfem_gpu.h``): :meth:`assemble` (all frequencies at once),
+:meth:`solve` (replaces zmumps), :meth:`impedance` (receiver Z / rho / phi), plus the
+parity hooks :meth:`numbering`, :meth:`export_coo`, :meth:`export_rhs`,
+:meth:`element_matrices` and :meth:`spmv`.
+
+Errors: every C-ABI status other than 0 raises :class:`MVFError` carrying the
+library's message (the reference prints and ``stop``s).  There is no CPU fallback:
+constructing a problem without the CUDA library or a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+MVF_OK, E_ARG, E_CUDA, E_SINGULAR, E_NOCONV, E_STATE, E_RECEIVER, E_NOMEM, E_UNSUPPORTED = 0, -1, -2, -3, -4, -5, -6, -7, -8
+MODE_MIXED, MODE_FP64 = 0, 1
+
+
+class MVFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"movfem_gpu error {code}: {msg}")
+        self.code = code
+
+
+class _Mesh(ctypes.Structure):
+    _fields_ = [
+        ("nodes_per_elem", ctypes.c_int32), ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("xp", ctypes.c_void_p), ("yp", ctypes.c_void_p), ("zp", ctypes.c_void_p), ("sigma", ctypes.c_void_p),
+        ("mu", ctypes.c_void_p), ("dirichlet", ctypes.c_int32), ("inimod", ctypes.c_int32),
+        ("gpml_sch", ctypes.c_int32), ("a0", ctypes.c_double), ("b0", ctypes.c_double), ("nn", ctypes.c_double),
+        ("nextd", ctypes.c_int32), ("nzl_top", ctypes.c_int32), ("nzl_air", ctypes.c_int32),
+        ("ztop", ctypes.c_double), ("quirks", ctypes.c_int32),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("outer_iters", ctypes.c_int32), ("inner_iters", ctypes.c_int32), ("rel_residual", ctypes.c_double),
+                ("seconds", ctypes.c_double), ("bytes_moved", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numbering", "mvf_set_sigma",
+           "mvf_assemble", "mvf_export_coo", "mvf_export_rhs", "mvf_element_matrices", "mvf_solve",
+           "mvf_impedance", "mvf_spmv"]
+
+_lib = None
+
+
+def library_path(build: bool = True) -> str:
+    return _build.build() if build else _build.LIB
+
+
+def load(build: bool = True):
+    """Load libmovfem_gpu.so (building it first if stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path(build)
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library missing: {path}")
+    L = ctypes.CDLL(path)
+    P, I32, I64, D = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    L.mvf_create.argtypes = [ctypes.POINTER(P), P, I32]
+    L.mvf_create.restype = ctypes.c_int
+    L.mvf_destroy.argtypes = [P]
+    L.mvf_destroy.restype = None
+    L.mvf_last_error.argtypes = [P]
+    L.mvf_last_error.restype = ctypes.c_char_p
+    L.mvf_sizes.argtypes = [P, P, P, P, P, P]
+    L.mvf_numbering.argtypes = [P, P]
+    L.mvf_set_sigma.argtypes = [P, P]
+    L.mvf_assemble.argtypes = [P, I32, P, P, I32]
+    L.mvf_export_coo.argtypes = [P, I32, P, P, P, P]
+    L.mvf_export_rhs.argtypes = [P, I32, P]
+    L.mvf_element_matrices.argtypes = [P, I64, I64, I32, P, P, P]
+    L.mvf_solve.argtypes = [P, P, D, I32, I32, P]
+    L.mvf_impedance.argtypes = [P, I32, P, P, P, P, P, P, P]
+    L.mvf_spmv.argtypes = [P, I32, P, P]
+    for n in EXPORTS:
+        if n not in ("mvf_destroy", "mvf_last_error", "mvf_create"):
+            getattr(L, n).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class MTProblem:
+    """One model on the GPU (the reference's module state after ``initialize_vfem``)."""
+
+    def __init__(self, mesh, device: int = -1):
+        self.L = load()
+        self.mesh = mesh
+        xp = np.ascontiguousarray(mesh.xp, dtype=np.float64)
+        yp = np.ascontiguousarray(mesh.yp, dtype=np.float64)
+        zp = np.ascontiguousarray(mesh.zp, dtype=np.float64)
+        sg = np.ascontiguousarray(mesh.sigma, dtype=np.complex128)
+        mu = np.ascontiguousarray(mesh.mu, dtype=np.float64)
+        m = _Mesh(mesh.nodes_per_elem, mesh.nx, mesh.ny, mesh.nz, _p(xp), _p(yp), _p(zp), _p(sg), _p(mu),
+                  mesh.dirichlet, mesh.inimod, mesh.gpml_sch, mesh.a0, mesh.b0, mesh.nn, mesh.nextd, mesh.nzl_top,
+                  mesh.nzl_air, mesh.ztop, mesh.quirks)
+        h = ctypes.c_void_p()
+        rc = self.L.mvf_create(ctypes.byref(h), ctypes.byref(m), device)
+        self.h = h
+        if rc != 0:
+            msg = self.L.mvf_last_error(h).decode()
+            self.L.mvf_destroy(h)
+            self.h = None
+            raise MVFError(rc, msg)
+        nne = ctypes.c_int32()
+        nnz = ctypes.c_int64()
+        nlo = ctypes.c_int64()
+        me = ctypes.c_int32()
+        ne = ctypes.c_int64()
+        self._chk(self.L.mvf_sizes(h, ctypes.byref(nne), ctypes.byref(nnz), ctypes.byref(nlo), ctypes.byref(me),
+                                   ctypes.byref(ne)))
+        self.nne, self.nnz, self.nnz_lower, self.me, self.ne = nne.value, nnz.value, nlo.value, me.value, ne.value
+        self.omega = None
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise MVFError(rc, self.L.mvf_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.L.mvf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def numbering(self):
+        gne = np.empty((self.me, self.ne), dtype=np.int32)
+        self._chk(self.L.mvf_numbering(self.h, _p(gne)))
+        return gne
+
+    def set_sigma(self, sigma):
+        s = np.ascontiguousarray(sigma, dtype=np.complex128)
+        self._chk(self.L.mvf_set_sigma(self.h, _p(s)))
+
+    def assemble(self, omega, sigma_f=None, ifreq0: int = 0):
+        om = np.ascontiguousarray(np.atleast_1d(omega), dtype=np.float64)
+        sf = None if sigma_f is None else np.ascontiguousarray(sigma_f, dtype=np.complex128)
+        self._chk(self.L.mvf_assemble(self.h, om.size, _p(om), _p(sf), ifreq0))
+        self.omega = om
+
+    def export_coo(self, f: int = 0):
+        n = ctypes.c_int64()
+        self._chk(self.L.mvf_export_coo(self.h, f, None, None, None, ctypes.byref(n)))
+        ia = np.empty(n.value, dtype=np.int32)
+        ja = np.empty(n.value, dtype=np.int32)
+        a = np.empty(n.value, dtype=np.complex128)
+        self._chk(self.L.mvf_export_coo(self.h, f, _p(ia), _p(ja), _p(a), ctypes.byref(n)))
+        return ia, ja, a
+
+    def export_rhs(self, f: int = 0):
+        b = np.empty((2, self.nne), dtype=np.complex128)
+        self._chk(self.L.mvf_export_rhs(self.h, f, _p(b)))
+        return b
+
+    def element_matrices(self, e0: int, count: int, f: int = 0):
+        K = np.empty((count, self.me, self.me))
+        M = np.empty((count, self.me, self.me))
+        b = np.empty((count, self.me, 2), dtype=np.complex128)
+        self._chk(self.L.mvf_element_matrices(self.h, e0, count, f, _p(K), _p(M), _p(b)))
+        return K, M, b
+
+    def solve(self, rhs=None, tol: float = 1e-10, mode: int = MODE_MIXED, max_iters: int = 5000,
+              raise_noconv: bool = True):
+        """Solve every assembled frequency and both polarisations.  Returns the
+        solutions [nfreq, 2, nne] and the solver statistics."""
+        if self.omega is None:
+            self._chk(self.L.mvf_solve(self.h, None, tol, mode, max_iters, None))
+        nf = self.omega.size
+        if rhs is None:
+            buf = np.stack([self.export_rhs(f) for f in range(nf)])
+        else:
+            buf = np.ascontiguousarray(rhs, dtype=np.complex128).reshape(nf, 2, self.nne).copy()
+        st = Stats()
+        rc = self.L.mvf_solve(self.h, _p(buf), tol, mode, max_iters, ctypes.byref(st))
+        if not (rc == E_NOCONV and not raise_noconv):
+            self._chk(rc)
+        return buf, st.as_dict()
+
+    def impedance(self, rx=None, with_fields: bool = False):
+        rx = self.mesh.rx if rx is None else np.asarray(rx, dtype=np.float64)
+        xr = np.ascontiguousarray(rx[:, 0])
+        yr = np.ascontiguousarray(rx[:, 1])
+        nf, nrx = self.omega.size, xr.size
+        Z = np.empty((nf, nrx, 4), dtype=np.complex128)
+        rho = np.empty((nf, nrx, 4))
+        phi = np.empty((nf, nrx, 4))
+        E = np.empty((nf, nrx, 2, 3), dtype=np.complex128) if with_fields else None
+        H = np.empty((nf, nrx, 2, 3), dtype=np.complex128) if with_fields else None
+        self._chk(self.L.mvf_impedance(self.h, nrx, _p(xr), _p(yr), _p(Z), _p(rho), _p(phi), _p(E), _p(H)))
+        return (Z, rho, phi, E, H) if with_fields else (Z, rho, phi)
+
+    def spmv(self, f: int, x):
+        xx = np.ascontiguousarray(x, dtype=np.complex128).reshape(2, self.nne)
+        y = np.empty_like(xx)
+        self._chk(self.L.mvf_spmv(self.h, f, _p(xx), _p(y)))
+        return y

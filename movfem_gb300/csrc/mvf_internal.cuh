@@ -1,0 +1,123 @@
+// mvf_internal.cuh -- context and shared declarations of the MoVFEM GB300 library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/movfem_gpu.h"
+#include "mvf_basis.cuh"
+
+#define MVF_MAX_NODES 27
+#define MVF_MAX_ME 54
+#define MVF_MAX_GP 27
+#define MVF_MAX_FREQ 16
+
+namespace mvf {
+
+// Element-order constants and tables evaluated at the Gauss points.
+struct OrderTables {
+    int mn = 0, me = 0, nord = 0, ngp = 0;
+    int edge_node[MVF_MAX_ME];  // 0-based node of each edge DOF (mx_edge_dir(:,1))
+    int edge_dir[MVF_MAX_ME];   // 0-based direction (mx_edge_dir(:,2))
+    int face_cnt = 0;           // DOFs per face
+    int face_src[3][12];        // DOFs on the +z, +y, +x face (0-based)
+    int face_dst[3][12];        // the same DOFs in the neighbour across that face
+    double gp[MVF_MAX_GP][4];   // xi, eta, zeta, weight (integration.f90:267-279)
+    // nodal N and dN/dxi at the Gauss points [g][node] / [g][node][3]
+    std::vector<double> N, dN;
+    // edge factor L and dL/dxi at the Gauss points [g][edge] / [g][edge][3]
+    std::vector<double> L, dL;
+    // discrete gradient of the element: grad N_n = sum_j G[j][n] * (edge basis j)
+    double G[MVF_MAX_ME][MVF_MAX_NODES];
+};
+
+// One set of real matrices K, M sharing the CSR pattern: either one per model
+// (frequency-independent Dirichlet assembly) or one per frequency (GPML).
+struct MatrixSet {
+    double *K64 = nullptr, *M64 = nullptr;  // [nnz]
+    float *K32 = nullptr, *M32 = nullptr;   // [nnz]
+    double *kphi = nullptr, *mphi = nullptr, *mabs = nullptr;  // gradient-node diagonals [ngn]
+    int first_freq = 0, nfreq = 0;          // frequencies that use this set
+};
+
+struct Device {
+    // model
+    double *xp = nullptr, *yp = nullptr, *zp = nullptr;
+    double *sigma = nullptr;   // [npt][6][2] current
+    double *sigma_f = nullptr; // [nfreq][npt][6][2] per frequency (optional)
+    double *mu = nullptr;      // [npt][6]
+    int32_t *gne = nullptr;    // [ne][me] element-major
+    int32_t *elem_color = nullptr;  // elements sorted by colour
+    // tables
+    double *N = nullptr, *dN = nullptr, *L = nullptr, *dL = nullptr, *gp = nullptr;
+    double *Gloc = nullptr;    // [me][mn]
+    int32_t *edge_node = nullptr, *edge_dir = nullptr;
+    // CSR (full, both triangles) and discrete gradient
+    int64_t *rowptr = nullptr;
+    int32_t *col = nullptr;
+    int64_t *grow = nullptr;   // G: [nne+1]
+    int32_t *gcol = nullptr;
+    float *gval = nullptr;
+    int64_t *gtrow = nullptr;  // G^T: [ngn+1]
+    int32_t *gtcol = nullptr;
+    float *gtval = nullptr;
+    int32_t *node_gidx = nullptr;  // grid node -> gradient node index or -1
+    // right-hand sides and solutions: [nfreq][2][nne] complex
+    double *rhs = nullptr;
+    double *x = nullptr;
+    // element matrices of the last assembly, kept for the parity hook
+    double *Ke = nullptr, *Me = nullptr, *be = nullptr;
+};
+
+struct Ctx {
+    mvf_mesh mesh{};
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    OrderTables T;
+    int64_t nnx = 0, nny = 0, nnz_nodes = 0, npt = 0, ne = 0;
+    int32_t nne = 0;
+    int64_t nnz = 0, nnz_lower = 0;
+    int32_t ngn = 0;  // gradient nodes
+    std::vector<int32_t> gne_h;  // [ne][me]
+    std::vector<double> xp_h, yp_h, zp_h;  // host copies of the coordinates
+    std::vector<int64_t> color_off;  // 9 offsets into elem_color
+    Device d;
+    // assembly state
+    int nfreq = 0;
+    double omega[MVF_MAX_FREQ] = {0};
+    int ifreq0 = 0;
+    std::vector<MatrixSet> sets;
+    bool assembled = false, solved = false;
+    bool keep_elements = false;
+    int64_t ke_count = 0;
+};
+
+int fail(Ctx *c, int code, const std::string &msg);
+int cuda_fail(Ctx *c, cudaError_t e, const char *what);
+int64_t element_node(const Ctx &c, int ie, int je, int ke, int l);
+int element_matrices(Ctx *c, int64_t e0, int64_t count, int f, double *K, double *M, double *b);
+
+#define MVF_CUDA(c, call)                                         \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return ::mvf::cuda_fail((c), _e, #call); \
+    } while (0)
+
+void build_tables(int mn, int quirks, OrderTables &T);
+
+// assembly (mvf_assemble.cu)
+int assemble_set(Ctx *c, MatrixSet &S, bool gpml, int fset);
+int assemble_rhs(Ctx *c);
+void free_sets(Ctx *c);
+
+}  // namespace mvf
+
+struct mvf_ctx {
+    mvf::Ctx c;
+};

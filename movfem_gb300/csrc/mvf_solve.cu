@@ -1,0 +1,768 @@
+// mvf_solve.cu -- the replacement of the MUMPS solve (zmumps job=6,
+// MoVFEM_3DMT.f90:113-115): right-preconditioned flexible GMRES on the GPU.
+//
+// Right-hand sides that share a matrix set are solved together: vectors are stored
+// [row][rhs] so one pass over K and M (A_r = K + i w_r M, integration.f90:76-86)
+// serves every right-hand side.  Preconditioner: z = D^-1 r + G Dphi^-1 G^T r, where D
+// is the diagonal of A_r, G the discrete gradient of the edge space and Dphi the
+// diagonal of G^T A_r G (the curl-curl operator vanishes on gradients, so Jacobi alone
+// stalls on them; nodes whose Dphi vanishes -- air, where Re(sigma)=0 -- are left out).
+// Mode 0 runs the Krylov method in complex FP32 with FP64 reductions and an FP64
+// Hessenberg least-squares problem inside FP64 iterative refinement (true residual
+// b - A x in FP64).  Mode 1 is the plain FP64 method, one right-hand side at a time.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "mvf_internal.cuh"
+
+namespace mvf {
+
+template <class T>
+struct C2;
+template <>
+struct C2<float> {
+    using V = float2;
+};
+template <>
+struct C2<double> {
+    using V = double2;
+};
+
+constexpr int MAXR = 32;  // right-hand sides per batch
+
+struct SolveParams {
+    double omega[MAXR];
+    double w32[MAXR];
+};
+__constant__ SolveParams c_sp;
+
+// y = A x (beta = 0) or y = b - A x (sub = 1) for R right-hand sides sharing K, M.
+// One warp per row; lane l handles rhs l % R over the nonzeros k = l / R + s*(32/R).
+template <class T, class TV, int R>
+__global__ void __launch_bounds__(256) spmm_km(int32_t n, const int64_t *__restrict__ rowptr,
+                                                const int32_t *__restrict__ col, const T *__restrict__ K,
+                                                const T *__restrict__ M, const TV *__restrict__ x,
+                                                const TV *__restrict__ b, TV *__restrict__ y, int use_w32) {
+    constexpr int SL = 32 / R;
+    const int lane = threadIdx.x & 31;
+    const int r = lane % R, s = lane / R;
+    const T w = use_w32 ? (T)c_sp.w32[r] : (T)c_sp.omega[r];
+    for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n;
+         row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int64_t k0 = rowptr[row], k1 = rowptr[row + 1];
+        T ar = 0, ai = 0, br = 0, bi = 0;
+        for (int64_t k = k0 + s; k < k1; k += SL) {
+            const T kv = K[k], mv = M[k];
+            const TV xv = x[(int64_t)col[k] * R + r];
+            // (K + i w M)(xr + i xi)
+            ar += kv * xv.x;
+            ai += kv * xv.y;
+            br += mv * xv.x;
+            bi += mv * xv.y;
+        }
+        T yr = ar - w * bi, yi = ai + w * br;
+#pragma unroll
+        for (int o = 16; o >= R; o >>= 1) {
+            yr += __shfl_down_sync(0xffffffffu, yr, o);
+            yi += __shfl_down_sync(0xffffffffu, yi, o);
+        }
+        if (s == 0) {
+            TV out;
+            if (b) {
+                const TV bv = b[row * R + r];
+                out.x = bv.x - yr;
+                out.y = bv.y - yi;
+            } else {
+                out.x = yr;
+                out.y = yi;
+            }
+            y[row * R + r] = out;
+        }
+    }
+}
+
+// diagonal entries of K and M
+__global__ void extract_diag(int32_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+                             const double *__restrict__ K, const double *__restrict__ M, double *__restrict__ kd,
+                             double *__restrict__ md) {
+    for (int32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        double a = 0, b = 0;
+        for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+            if (col[k] == r) { a = K[k]; b = M[k]; }
+        kd[r] = a;
+        md[r] = b;
+    }
+}
+
+// inverse diagonals of the preconditioner for each rhs: dinv [n][R], pinv [ngn][R]
+__global__ void build_inverse_diag(int32_t n, int32_t ngn, int R, const double *__restrict__ kd,
+                                   const double *__restrict__ md, const double *__restrict__ kphi,
+                                   const double *__restrict__ mphi, const double *__restrict__ mabs,
+                                   double2 *__restrict__ dinv, double2 *__restrict__ pinv) {
+    const int64_t tot = ((int64_t)n + ngn) * R;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(t % R);
+        const int64_t i = t / R;
+        const double w = c_sp.w32[r];
+        if (i < n) {
+            const double a = kd[i], b = w * md[i];
+            const double s = a * a + b * b;
+            dinv[i * R + r] = s > 0 ? make_double2(a / s, -b / s) : make_double2(0.0, 0.0);
+        } else {
+            const int64_t j = i - n;
+            const double a = kphi[j], b = w * mphi[j];
+            const double scale = fabs(kphi[j]) + w * mabs[j];
+            const double s = a * a + b * b;
+            // keep a gradient node only where the mass part is a real fraction of its scale
+            const bool keep = scale > 0 && w * fabs(mphi[j]) > 1e-8 * scale && s > 0;
+            pinv[j * R + r] = keep ? make_double2(a / s, -b / s) : make_double2(0.0, 0.0);
+        }
+    }
+}
+
+// t = Pinv .* (G^T r)   (gradient nodes)
+template <class TV>
+__global__ void grad_t(int32_t ngn, int R, const int64_t *__restrict__ gtrow, const int32_t *__restrict__ gtcol,
+                       const float *__restrict__ gtval, const TV *__restrict__ r, const double2 *__restrict__ pinv,
+                       TV *__restrict__ t) {
+    const int64_t tot = (int64_t)ngn * R;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = q / R;
+        const int rr = (int)(q % R);
+        double sr = 0, si = 0;
+        for (int64_t k = gtrow[j]; k < gtrow[j + 1]; ++k) {
+            const TV v = r[(int64_t)gtcol[k] * R + rr];
+            sr += gtval[k] * (double)v.x;
+            si += gtval[k] * (double)v.y;
+        }
+        const double2 p = pinv[q];
+        TV o;
+        o.x = (decltype(o.x))(p.x * sr - p.y * si);
+        o.y = (decltype(o.y))(p.x * si + p.y * sr);
+        t[q] = o;
+    }
+}
+
+// z = Dinv .* r + G t
+template <class TV>
+__global__ void apply_prec(int32_t n, int R, const int64_t *__restrict__ grow, const int32_t *__restrict__ gcol,
+                           const float *__restrict__ gval, const TV *__restrict__ r, const double2 *__restrict__ dinv,
+                           const TV *__restrict__ t, TV *__restrict__ z) {
+    const int64_t tot = (int64_t)n * R;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = q / R;
+        const int rr = (int)(q % R);
+        const TV v = r[q];
+        const double2 d = dinv[q];
+        double zr = d.x * v.x - d.y * v.y, zi = d.x * v.y + d.y * v.x;
+        for (int64_t k = grow[i]; k < grow[i + 1]; ++k) {
+            const TV tv = t[(int64_t)gcol[k] * R + rr];
+            zr += gval[k] * (double)tv.x;
+            zi += gval[k] * (double)tv.y;
+        }
+        TV o;
+        o.x = (decltype(o.x))zr;
+        o.y = (decltype(o.y))zi;
+        z[q] = o;
+    }
+}
+
+// Partial sums of conj(V_j) . w for j < k and all rhs (FP64 accumulation), one row
+// of partial[block][j][r] per block.  Threads keep 8 projections in registers while
+// streaming w once per group of 8 basis vectors; lanes with the same rhs are combined
+// with shuffles, warps through shared-memory atomics ([k][R] doubles).
+template <class TV>
+__global__ void __launch_bounds__(256) multidot(int32_t n, int R, int k, const TV *__restrict__ V, int64_t vstride,
+                                                 const TV *__restrict__ w, double2 *__restrict__ partial) {
+    extern __shared__ double red[];  // [k*R][2]
+    constexpr int JC = 8;
+    const int lane = threadIdx.x & 31;
+    const int kr = k * R;
+    for (int t = threadIdx.x; t < 2 * kr; t += blockDim.x) red[t] = 0.0;
+    __syncthreads();
+    const int r = threadIdx.x % R;  // R divides 32 and blockDim, so fixed per thread
+    const int64_t tot = (int64_t)n * R;
+    for (int j0 = 0; j0 < k; j0 += JC) {
+        const int jn = min(JC, k - j0);
+        double sr[JC], si[JC];
+#pragma unroll
+        for (int q = 0; q < JC; ++q) sr[q] = si[q] = 0.0;
+        for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+            const TV b = w[q];
+#pragma unroll
+            for (int jj = 0; jj < JC; ++jj) {
+                if (jj < jn) {
+                    const TV a = V[(int64_t)(j0 + jj) * vstride + q];
+                    sr[jj] += (double)a.x * b.x + (double)a.y * b.y;
+                    si[jj] += (double)a.x * b.y - (double)a.y * b.x;
+                }
+            }
+        }
+#pragma unroll
+        for (int jj = 0; jj < JC; ++jj) {
+            double xr = sr[jj], xi = si[jj];
+            for (int o = 16; o >= R; o >>= 1) {
+                xr += __shfl_down_sync(0xffffffffu, xr, o);
+                xi += __shfl_down_sync(0xffffffffu, xi, o);
+            }
+            if (jj < jn && lane < R) {
+                atomicAdd(&red[2 * ((j0 + jj) * R + r)], xr);
+                atomicAdd(&red[2 * ((j0 + jj) * R + r) + 1], xi);
+            }
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kr; t += blockDim.x)
+        partial[(int64_t)blockIdx.x * kr + t] = make_double2(red[2 * t], red[2 * t + 1]);
+}
+
+// sum the block partials: h[t] (+)= sum_b partial[b][t]
+__global__ void reduce_partials(int nblocks, int kr, const double2 *__restrict__ partial, double2 *__restrict__ h,
+                                int accumulate) {
+    const int t = blockIdx.x;
+    double sr = 0, si = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        sr += partial[(int64_t)b * kr + t].x;
+        si += partial[(int64_t)b * kr + t].y;
+    }
+    __shared__ double2 s[256];
+    s[threadIdx.x] = make_double2(sr, si);
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            s[threadIdx.x].x += s[threadIdx.x + o].x;
+            s[threadIdx.x].y += s[threadIdx.x + o].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (accumulate) {
+            h[t].x += s[0].x;
+            h[t].y += s[0].y;
+        } else {
+            h[t] = s[0];
+        }
+    }
+}
+
+// w -= sum_j c[j][r] V_j  (c is the last projection, FP64)
+template <class TV>
+__global__ void axpy_multi(int32_t n, int R, int k, const TV *__restrict__ V, int64_t vstride,
+                           const double2 *__restrict__ c, TV *__restrict__ w) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)n * R;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(q % R);
+        TV o = w[q];
+        double orr = o.x, oi = o.y;
+        for (int j = 0; j < k; ++j) {
+            const TV v = V[(int64_t)j * vstride + q];
+            const double2 h = c[j * R + r];
+            orr -= h.x * v.x - h.y * v.y;
+            oi -= h.x * v.y + h.y * v.x;
+        }
+        o.x = (decltype(o.x))orr;
+        o.y = (decltype(o.y))oi;
+        w[q] = o;
+    }
+}
+
+// v = w / nrm[r]  (nrm from a 1-vector multidot of w with itself)
+template <class TV>
+__global__ void scale_into(int32_t n, int R, const TV *__restrict__ w, const double2 *__restrict__ nrm2,
+                           TV *__restrict__ v) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)n * R;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(q % R);
+        const double nr = sqrt(fmax(nrm2[r].x, 0.0));
+        const double s = nr > 0 ? 1.0 / nr : 0.0;
+        TV o = w[q];
+        o.x = (decltype(o.x))(o.x * s);
+        o.y = (decltype(o.y))(o.y * s);
+        v[q] = o;
+    }
+}
+
+// Hessenberg column k for each rhs: h[0..k] from the two CGS passes (hc), h[k+1] =
+// ||w||; apply the previous Givens rotations, form the new one, update g.
+struct Hess {
+    double2 H[64][65];  // H[row][col], (m+1) x m
+    double2 cs[64];     // cos (real) packed in .x; sin complex
+    double2 sn[64];
+    double2 g[65];
+    double beta;
+    int active;
+};
+
+__global__ void hessenberg_step(int R, int k, const double2 *__restrict__ hc, const double2 *__restrict__ wn2, Hess *hs) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    Hess &S = hs[r];
+    for (int i = 0; i <= k; ++i) S.H[i][k] = hc[i * R + r];
+    S.H[k + 1][k] = make_double2(sqrt(fmax(wn2[r].x, 0.0)), 0.0);
+    // previous rotations: [c s; -conj(s) c] with c real
+    for (int i = 0; i < k; ++i) {
+        const double c = S.cs[i].x;
+        const double2 s = S.sn[i];
+        const double2 a = S.H[i][k], b = S.H[i + 1][k];
+        double2 t1, t2;
+        t1.x = c * a.x + (s.x * b.x - s.y * b.y);
+        t1.y = c * a.y + (s.x * b.y + s.y * b.x);
+        t2.x = -(s.x * a.x + s.y * a.y) + c * b.x;
+        t2.y = -(s.x * a.y - s.y * a.x) + c * b.y;
+        S.H[i][k] = t1;
+        S.H[i + 1][k] = t2;
+    }
+    const double2 a = S.H[k][k];
+    const double bb = S.H[k + 1][k].x;  // real and >= 0
+    const double na = hypot(a.x, a.y);
+    double c;
+    double2 s;
+    if (bb == 0.0) { c = 1.0; s = make_double2(0.0, 0.0); }
+    else if (na == 0.0) { c = 0.0; s = make_double2(1.0, 0.0); }
+    else {
+        const double nrm = hypot(na, bb);
+        c = na / nrm;
+        // s = (a/|a|) * conj(b) / nrm  with b real
+        s = make_double2(a.x / na * bb / nrm, a.y / na * bb / nrm);
+    }
+    S.cs[k] = make_double2(c, 0.0);
+    S.sn[k] = s;
+    // H[k][k] = c a + s b
+    S.H[k][k] = make_double2(c * a.x + s.x * bb, c * a.y + s.y * bb);
+    S.H[k + 1][k] = make_double2(0.0, 0.0);
+    const double2 gk = S.g[k];
+    S.g[k] = make_double2(c * gk.x, c * gk.y);
+    // g[k+1] = -conj(s) g[k]
+    S.g[k + 1] = make_double2(-(s.x * gk.x + s.y * gk.y), -(s.x * gk.y - s.y * gk.x));
+}
+
+__global__ void hessenberg_init(int R, const double2 *__restrict__ rn2, Hess *hs) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const double b = sqrt(fmax(rn2[r].x, 0.0));
+    hs[r].beta = b;
+    hs[r].g[0] = make_double2(b, 0.0);
+    for (int i = 1; i < 65; ++i) hs[r].g[i] = make_double2(0.0, 0.0);
+}
+
+// back substitution: y = H(0:k,0:k)^-1 g(0:k), stored in yout[j][r]
+__global__ void hessenberg_solve(int R, int k, Hess *hs, double2 *__restrict__ yout) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    Hess &S = hs[r];
+    double2 y[64];
+    for (int i = k - 1; i >= 0; --i) {
+        double2 t = S.g[i];
+        for (int j = i + 1; j < k; ++j) {
+            const double2 h = S.H[i][j];
+            t.x -= h.x * y[j].x - h.y * y[j].y;
+            t.y -= h.x * y[j].y + h.y * y[j].x;
+        }
+        const double2 d = S.H[i][i];
+        const double dd = d.x * d.x + d.y * d.y;
+        y[i] = dd > 0 ? make_double2((t.x * d.x + t.y * d.y) / dd, (t.y * d.x - t.x * d.y) / dd) : make_double2(0, 0);
+    }
+    for (int i = 0; i < k; ++i) yout[i * R + r] = y[i];
+}
+
+// x += sum_j y[j][r] Z_j   (x in FP64; Z in the Krylov precision)
+template <class TV, class XV>
+__global__ void update_x(int32_t n, int R, int k, const TV *__restrict__ Z, int64_t zstride,
+                         const double2 *__restrict__ y, XV *__restrict__ x, int xstride_r, int xoff) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)n * R;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(q % R);
+        double sr = 0, si = 0;
+        for (int j = 0; j < k; ++j) {
+            const TV z = Z[(int64_t)j * zstride + q];
+            const double2 c = y[j * R + r];
+            sr += c.x * z.x - c.y * z.y;
+            si += c.x * z.y + c.y * z.x;
+        }
+        const int64_t i = q / R;
+        XV &o = x[i * xstride_r + xoff + r];
+        o.x += sr;
+        o.y += si;
+    }
+}
+
+template <class TV>
+__global__ void cast_vec(int64_t n, const double2 *__restrict__ a, TV *__restrict__ b, double scale) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        TV o;
+        o.x = (decltype(o.x))(a[q].x * scale);
+        o.y = (decltype(o.y))(a[q].y * scale);
+        b[q] = o;
+    }
+}
+
+// gather rhs [f][p][n] -> [n][R] and scatter back
+__global__ void gather_rhs(int32_t n, int R, int f0, const double2 *__restrict__ src, double2 *__restrict__ dst) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)n * R;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(q % R);
+        const int64_t i = q / R;
+        dst[q] = src[((int64_t)(f0 * 2 + r)) * n + i];
+    }
+}
+__global__ void scatter_sol(int32_t n, int R, int f0, const double2 *__restrict__ src, double2 *__restrict__ dst) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)n * R;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(q % R);
+        const int64_t i = q / R;
+        dst[((int64_t)(f0 * 2 + r)) * n + i] = src[q];
+    }
+}
+
+// ------------------------------------------------------------------------ host side
+struct Work {
+    int R = 0, m = 0;
+    int32_t n = 0;
+    int nblocks = 0;
+    void *V = nullptr, *Z = nullptr, *w = nullptr, *t = nullptr;  // Krylov precision
+    double2 *x64 = nullptr, *b64 = nullptr, *r64 = nullptr;       // [n][R]
+    double2 *dinv = nullptr, *pinv = nullptr;
+    double2 *partial = nullptr, *hc = nullptr, *htmp = nullptr, *nrm = nullptr, *y = nullptr;
+    double *kd = nullptr, *md = nullptr;
+    Hess *hs = nullptr;
+    size_t vb = 0;
+};
+
+static void free_work(Work &W) {
+    void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs};
+    for (void *q : p)
+        if (q) cudaFree(q);
+    W = Work{};
+}
+
+template <class T>
+static int alloc_work(Ctx *c, Work &W, int R, int m) {
+    using TV = typename C2<T>::V;
+    W.R = R;
+    W.m = m;
+    W.n = c->nne;
+    W.nblocks = 152 * 4;
+    const size_t nv = (size_t)W.n * R;
+    W.vb = nv * sizeof(TV);
+    MVF_CUDA(c, cudaMalloc(&W.V, W.vb * (m + 1)));
+    MVF_CUDA(c, cudaMalloc(&W.Z, W.vb * m));
+    MVF_CUDA(c, cudaMalloc(&W.w, W.vb));
+    MVF_CUDA(c, cudaMalloc(&W.t, (size_t)std::max(c->ngn, 1) * R * sizeof(TV)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.x64, nv * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.b64, nv * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.r64, nv * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.dinv, nv * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.pinv, (size_t)std::max(c->ngn, 1) * R * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.partial, (size_t)W.nblocks * (m + 1) * R * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.hc, (size_t)(m + 1) * R * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.htmp, (size_t)(m + 1) * R * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.nrm, (size_t)R * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.y, (size_t)(m + 1) * R * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.kd, (size_t)W.n * sizeof(double)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.md, (size_t)W.n * sizeof(double)));
+    MVF_CUDA(c, cudaMalloc((void **)&W.hs, (size_t)R * sizeof(Hess)));
+    return 0;
+}
+
+template <class T, class TV>
+static void launch_spmm(Ctx *c, int R, const T *K, const T *M, const TV *x, const TV *b, TV *y, int use_w32) {
+    const int threads = 256;
+    const int64_t rows_per_block = threads / 32;
+    const unsigned grid = (unsigned)std::min<int64_t>((c->nne + rows_per_block - 1) / rows_per_block, 152 * 64);
+    switch (R) {
+        case 1: spmm_km<T, TV, 1><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+        case 2: spmm_km<T, TV, 2><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+        case 4: spmm_km<T, TV, 4><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+        case 8: spmm_km<T, TV, 8><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+        case 16: spmm_km<T, TV, 16><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+        default: spmm_km<T, TV, 32><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+    }
+}
+
+static unsigned grid_for(int64_t n) { return (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 32); }
+
+// Orthogonalise w against V_0..V_{k-1} (two classical Gram-Schmidt passes), write the
+// projections to W.hc[0..k) and ||w||^2 to W.nrm.
+template <class TV>
+static int cgs2(Ctx *c, Work &W, int k) {
+    const int R = W.R;
+    const TV *V = (const TV *)W.V;
+    TV *w = (TV *)W.w;
+    const int64_t vs = (int64_t)W.n * R;
+    for (int pass = 0; pass < 2; ++pass) {
+        const size_t sm = (size_t)k * R * sizeof(double2);
+        multidot<TV><<<W.nblocks, 256, sm, c->stream>>>(W.n, R, k, V, vs, w, W.partial);
+        reduce_partials<<<k * R, 256, 0, c->stream>>>(W.nblocks, k * R, W.partial, pass == 0 ? W.hc : W.htmp, 0);
+        axpy_multi<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, k, V, vs, pass == 0 ? W.hc : W.htmp, w);
+        if (pass == 1) {
+            // hc += htmp
+            reduce_partials<<<k * R, 256, 0, c->stream>>>(1, k * R, W.htmp, W.hc, 1);
+        }
+    }
+    multidot<TV><<<W.nblocks, 256, (size_t)R * sizeof(double2), c->stream>>>(W.n, R, 1, w, vs, w, W.partial);
+    reduce_partials<<<R, 256, 0, c->stream>>>(W.nblocks, R, W.partial, W.nrm, 0);
+    MVF_CUDA(c, cudaGetLastError());
+    return 0;
+}
+
+template <class TV>
+static void precondition(Ctx *c, Work &W, const TV *r, TV *z) {
+    const int R = W.R;
+    grad_t<TV><<<grid_for((int64_t)c->ngn * R), 256, 0, c->stream>>>(c->ngn, R, c->d.gtrow, c->d.gtcol, c->d.gtval, r,
+                                                                    W.pinv, (TV *)W.t);
+    apply_prec<TV><<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, c->d.grow, c->d.gcol, c->d.gval, r,
+                                                                     W.dinv, (const TV *)W.t, z);
+}
+
+// One FGMRES cycle (at most m iterations) on A d = rhs (Krylov precision TV) with
+// initial guess 0, adding the correction to x (FP64, [n][R]).  Returns iterations.
+template <class T>
+static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T>::V *rhs, double2 *x, double tol_abs_rel,
+                        int &iters, std::vector<double> &est) {
+    using TV = typename C2<T>::V;
+    const int R = W.R, m = W.m;
+    const int64_t vs = (int64_t)W.n * R;
+    TV *V = (TV *)W.V, *Z = (TV *)W.Z, *w = (TV *)W.w;
+    const T *K = std::is_same<T, float>::value ? (const T *)S.K32 : (const T *)S.K64;
+    const T *M = std::is_same<T, float>::value ? (const T *)S.M32 : (const T *)S.M64;
+    const int use_w32 = 1;
+    // V0 = rhs / ||rhs||
+    MVF_CUDA(c, cudaMemcpyAsync(w, rhs, W.vb, cudaMemcpyDeviceToDevice, c->stream));
+    multidot<TV><<<W.nblocks, 256, (size_t)R * sizeof(double2), c->stream>>>(W.n, R, 1, w, vs, w, W.partial);
+    reduce_partials<<<R, 256, 0, c->stream>>>(W.nblocks, R, W.partial, W.nrm, 0);
+    hessenberg_init<<<1, 32, 0, c->stream>>>(R, W.nrm, W.hs);
+    scale_into<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, w, W.nrm, V);
+    std::vector<Hess> hh(R);
+    std::vector<double> beta(R);
+    int k = 0;
+    for (k = 0; k < m; ++k) {
+        precondition<TV>(c, W, V + k * vs, Z + k * vs);
+        launch_spmm<T, TV>(c, R, K, M, Z + k * vs, (const TV *)nullptr, w, use_w32);
+        int rc = cgs2<TV>(c, W, k + 1);
+        if (rc) return rc;
+        hessenberg_step<<<1, 32, 0, c->stream>>>(R, k, W.hc, W.nrm, W.hs);
+        scale_into<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, w, W.nrm, V + (k + 1) * vs);
+        // check the residual estimate every 10 iterations and at the end
+        if ((k + 1) % 10 == 0 || k + 1 == m) {
+            MVF_CUDA(c, cudaMemcpyAsync(hh.data(), W.hs, sizeof(Hess) * R, cudaMemcpyDeviceToHost, c->stream));
+            MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+            bool all = true;
+            for (int r = 0; r < R; ++r) {
+                const double g = hypot(hh[r].g[k + 1].x, hh[r].g[k + 1].y);
+                est[r] = hh[r].beta > 0 ? g / hh[r].beta : 0.0;
+                if (est[r] > tol_abs_rel) all = false;
+            }
+            if (all) { ++k; break; }
+        }
+    }
+    hessenberg_solve<<<1, 32, 0, c->stream>>>(R, k, W.hs, W.y);
+    update_x<TV, double2><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, k, Z, vs, W.y, x, R, 0);
+    MVF_CUDA(c, cudaGetLastError());
+    iters += k;
+    return 0;
+}
+
+static int residual_norms(Ctx *c, Work &W, const MatrixSet &S, std::vector<double> &rel, std::vector<double> &bn) {
+    const int R = W.R;
+    const int64_t vs = (int64_t)W.n * R;
+    launch_spmm<double, double2>(c, R, S.K64, S.M64, W.x64, W.b64, W.r64, 1);
+    multidot<double2><<<W.nblocks, 256, (size_t)R * sizeof(double2), c->stream>>>(W.n, R, 1, W.r64, vs, W.r64, W.partial);
+    reduce_partials<<<R, 256, 0, c->stream>>>(W.nblocks, R, W.partial, W.nrm, 0);
+    std::vector<double2> h(R);
+    MVF_CUDA(c, cudaMemcpyAsync(h.data(), W.nrm, R * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+    MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int r = 0; r < R; ++r) rel[r] = bn[r] > 0 ? std::sqrt(std::max(h[r].x, 0.0)) / bn[r] : 0.0;
+    return 0;
+}
+
+// Solve the R = 2*nf right-hand sides of one matrix set.
+template <class T>
+static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int npol, double tol, int max_iters,
+                     mvf_stats *st, int m) {
+    using TV = typename C2<T>::V;
+    const int R = nfs * npol;
+    Work W;
+    int rc = alloc_work<T>(c, W, R, m);
+    if (rc) { free_work(W); return rc; }
+    SolveParams sp{};
+    for (int r = 0; r < R; ++r) {
+        const int f = f0 + r / npol;
+        sp.omega[r] = c->omega[f];
+        sp.w32[r] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
+    }
+    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    extract_diag<<<grid_for(c->nne), 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.K64, S.M64, W.kd, W.md);
+    build_inverse_diag<<<grid_for(((int64_t)c->nne + c->ngn) * R), 256, 0, c->stream>>>(
+        c->nne, c->ngn, R, W.kd, W.md, S.kphi, S.mphi, S.mabs, W.dinv, W.pinv);
+    // gather right-hand sides [f][p][n] -> [n][R]
+    if (npol == 2) {
+        gather_rhs<<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, f0, (const double2 *)c->d.rhs, W.b64);
+    } else {
+        // single rhs (f0, pol0)
+        MVF_CUDA(c, cudaMemcpyAsync(W.b64, (const double2 *)c->d.rhs + ((int64_t)f0 * 2 + pol0) * W.n,
+                                    (size_t)W.n * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    MVF_CUDA(c, cudaMemsetAsync(W.x64, 0, (size_t)W.n * R * sizeof(double2), c->stream));
+    std::vector<double> bn(R, 1.0), rel(R, 0.0), est(R, 0.0);
+    {
+        const int64_t vs = (int64_t)W.n * R;
+        multidot<double2><<<W.nblocks, 256, (size_t)R * sizeof(double2), c->stream>>>(W.n, R, 1, W.b64, vs, W.b64, W.partial);
+        reduce_partials<<<R, 256, 0, c->stream>>>(W.nblocks, R, W.partial, W.nrm, 0);
+        std::vector<double2> h(R);
+        MVF_CUDA(c, cudaMemcpyAsync(h.data(), W.nrm, R * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+        MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int r = 0; r < R; ++r) bn[r] = std::sqrt(std::max(h[r].x, 0.0));
+    }
+    int iters = 0, outer = 0;
+    const bool mixed = std::is_same<T, float>::value;
+    double worst = 1.0;
+    while (true) {
+        if ((rc = residual_norms(c, W, S, rel, bn))) break;
+        worst = 0;
+        for (int r = 0; r < R; ++r) worst = std::max(worst, rel[r]);
+        if (worst <= tol || iters >= max_iters) break;
+        ++outer;
+        // inner solve on the scaled residual in the Krylov precision
+        TV *rk = (TV *)W.w;  // reuse: cycle copies rhs into w first, so stage in V_m
+        TV *stage = (TV *)W.V + (int64_t)W.m * W.n * R;
+        cast_vec<TV><<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>((int64_t)W.n * R, W.r64, stage, 1.0);
+        (void)rk;
+        // the cycle writes V_0 from its rhs before V_m is reused, so the staging copy
+        // is consumed first
+        const double inner_tol = mixed ? std::max(tol / std::max(worst, 1e-300), 2e-5) : tol / std::max(worst, 1e-300);
+        if ((rc = fgmres_cycle<T>(c, W, S, stage, W.x64, inner_tol, iters, est))) break;
+    }
+    if (!rc) {
+        if (npol == 2)
+            scatter_sol<<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, f0, W.x64, (double2 *)c->d.x);
+        else
+            MVF_CUDA(c, cudaMemcpyAsync((double2 *)c->d.x + ((int64_t)f0 * 2 + pol0) * W.n, W.x64,
+                                        (size_t)W.n * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
+        MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    if (st) {
+        st->outer_iters = std::max(st->outer_iters, outer);
+        st->inner_iters = std::max(st->inner_iters, iters);
+        st->rel_residual = std::max(st->rel_residual, worst);
+    }
+    free_work(W);
+    if (!rc && worst > tol) return MVF_E_NOCONV;
+    return rc;
+}
+
+}  // namespace mvf
+
+using namespace mvf;
+
+extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mode, int32_t max_iters, mvf_stats *st) {
+    if (!xc) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble before solve");
+    if (!(tol > 0) || max_iters < 1) return fail(c, MVF_E_ARG, "tol > 0 and max_iters >= 1 required");
+    if (st) *st = mvf_stats{};
+    const size_t vb = (size_t)c->nfreq * 2 * c->nne * 2 * sizeof(double);
+    if (rhs_inout) MVF_CUDA(c, cudaMemcpy(c->d.rhs, rhs_inout, vb, cudaMemcpyHostToDevice));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->stream);
+    int rc = 0, noconv = 0;
+    for (const MatrixSet &S : c->sets) {
+        if (mode == 0) {
+            // all frequencies of the set and both polarisations in one batch
+            int r = solve_set<float>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, 40);
+            if (r == MVF_E_NOCONV) noconv = 1;
+            else if (r) { rc = r; break; }
+        } else {
+            for (int f = S.first_freq; f < S.first_freq + S.nfreq && !rc; ++f)
+                for (int p = 0; p < 2 && !rc; ++p) {
+                    int r = solve_set<double>(c, S, f, 1, p, 1, tol, max_iters, st, 40);
+                    if (r == MVF_E_NOCONV) noconv = 1;
+                    else if (r) rc = r;
+                }
+        }
+    }
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) st->seconds = ms * 1e-3;
+    if (rc) return rc;
+    if (rhs_inout) MVF_CUDA(c, cudaMemcpy(rhs_inout, c->d.x, vb, cudaMemcpyDeviceToHost));
+    c->solved = true;
+    if (noconv) return fail(c, MVF_E_NOCONV, "solver stopped at its iteration cap above tolerance");
+    return 0;
+}
+
+extern "C" int mvf_spmv(mvf_ctx *xc, int32_t f, const double *x, double *y) {
+    if (!xc || !x || !y) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
+    if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
+    const MatrixSet *S = nullptr;
+    for (const MatrixSet &s : c->sets)
+        if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
+    SolveParams sp{};
+    sp.omega[0] = sp.omega[1] = c->omega[f];
+    sp.w32[0] = sp.w32[1] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
+    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    double2 *dx, *dy, *tx, *ty;
+    const size_t nb = (size_t)c->nne * 2 * sizeof(double2);
+    MVF_CUDA(c, cudaMalloc((void **)&dx, nb));
+    MVF_CUDA(c, cudaMalloc((void **)&dy, nb));
+    MVF_CUDA(c, cudaMalloc((void **)&tx, nb));
+    MVF_CUDA(c, cudaMalloc((void **)&ty, nb));
+    MVF_CUDA(c, cudaMemcpyAsync(dx, x, nb, cudaMemcpyHostToDevice, c->stream));
+    gather_rhs<<<grid_for((int64_t)c->nne * 2), 256, 0, c->stream>>>(c->nne, 2, 0, dx, tx);
+    launch_spmm<double, double2>(c, 2, S->K64, S->M64, tx, (const double2 *)nullptr, ty, 1);
+    scatter_sol<<<grid_for((int64_t)c->nne * 2), 256, 0, c->stream>>>(c->nne, 2, 0, ty, dy);
+    MVF_CUDA(c, cudaMemcpyAsync(y, dy, nb, cudaMemcpyDeviceToHost, c->stream));
+    MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(dx); cudaFree(dy); cudaFree(tx); cudaFree(ty);
+    return 0;
+}
+
+extern "C" int mvf_export_rhs(const mvf_ctx *xc, int32_t f, double *rhs) {
+    if (!xc || !rhs) return MVF_E_ARG;
+    Ctx *c = const_cast<Ctx *>(&xc->c);
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
+    if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
+    MVF_CUDA(c, cudaMemcpy(rhs, c->d.rhs + (int64_t)f * 2 * c->nne * 2, (size_t)2 * c->nne * 2 * sizeof(double),
+                           cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+extern "C" int mvf_export_coo(const mvf_ctx *xc, int32_t f, int32_t *ia, int32_t *ja, double *a, int64_t *nnz) {
+    if (!xc || !nnz) return MVF_E_ARG;
+    Ctx *c = const_cast<Ctx *>(&xc->c);
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
+    if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
+    *nnz = c->nnz_lower;
+    if (!ia && !ja && !a) return 0;
+    if (!ia || !ja || !a) return fail(c, MVF_E_ARG, "ia, ja and a must all be given");
+    const MatrixSet *S = nullptr;
+    for (const MatrixSet &s : c->sets)
+        if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
+    std::vector<int64_t> rp(c->nne + 1);
+    std::vector<int32_t> cl(c->nnz);
+    std::vector<double> K(c->nnz), M(c->nnz);
+    MVF_CUDA(c, cudaMemcpy(rp.data(), c->d.rowptr, rp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    MVF_CUDA(c, cudaMemcpy(cl.data(), c->d.col, cl.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    MVF_CUDA(c, cudaMemcpy(K.data(), S->K64, K.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    MVF_CUDA(c, cudaMemcpy(M.data(), S->M64, M.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    const double w32 = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
+    int64_t q = 0;
+    for (int32_t r = 0; r < c->nne; ++r)
+        for (int64_t k = rp[r]; k < rp[r + 1]; ++k) {
+            if (cl[k] > r) continue;
+            ia[q] = r + 1;
+            ja[q] = cl[k] + 1;
+            a[2 * q] = K[k];
+            a[2 * q + 1] = w32 * M[k];
+            ++q;
+        }
+    return 0;
+}

@@ -1,0 +1,184 @@
+"""GPU parity tests: the CUDA library (through its C-ABI) against the oracle.
+
+Integer outputs (DOF numbering, boundary flags, CSR pattern) must be bit-exact.
+Element and global matrix values are FP64 on both sides: relative error <= 1e-10 of
+the largest entry.  Solutions: relative FP64 residual <= 1e-10 and impedance
+||Z - Z_oracle||_F / ||Z_oracle||_F <= 1e-6 per receiver against the oracle's direct
+solve.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from movfem_gb300 import api
+from movfem_gb300 import mesh as M
+from tests import models
+
+pytestmark = pytest.mark.gpu
+
+ORDERS = [8, 20, 27]
+
+
+def _problem(m):
+    return api.MTProblem(m)
+
+
+@pytest.mark.parametrize("mn", ORDERS)
+@pytest.mark.parametrize("dirichlet", [1, 0])
+def test_numbering_bit_exact(mn, dirichlet):
+    m = models.box(mn, n=(3, 4, 2), dirichlet=dirichlet, nextd=0 if dirichlet else 1)
+    p = _problem(m)
+    gne_ref, nne_ref = oracle.Oracle(m).numbering()
+    gne = p.numbering()
+    assert p.nne == nne_ref
+    assert np.array_equal(gne, gne_ref)
+
+
+@pytest.mark.parametrize("mn", ORDERS)
+@pytest.mark.parametrize("dirichlet", [1, 0])
+def test_pattern_equals_reference_coo(mn, dirichlet):
+    m = models.box(mn, n=(3, 3, 3), dirichlet=dirichlet, nextd=0 if dirichlet else 1)
+    p = _problem(m)
+    p.assemble([2 * math.pi * 0.5])
+    ia, ja, _ = p.export_coo(0)
+    o = oracle.Oracle(m)
+    ria, rja = o.coo_coords()
+    low = ria >= rja
+    ref = set(zip(ria[low].tolist(), rja[low].tolist()))
+    got = list(zip(ia.tolist(), ja.tolist()))
+    assert len(got) == len(ref) == p.nnz_lower
+    assert set(got) == ref
+    # row-major order
+    assert all(np.diff(ia.astype(np.int64) * (p.nne + 1) + ja) > 0)
+    assert p.nnz == 2 * p.nnz_lower - p.nne
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("mn", ORDERS)
+@pytest.mark.parametrize("kind", ["dirichlet", "dirichlet-aniso", "topo", "gpml-fang", "gpml-zhou"])
+def test_element_matrices(mn, kind):
+    if kind == "topo":
+        m = models.topo(mn)
+    elif kind.startswith("gpml"):
+        m = models.box(mn, n=(3, 3, 2), dirichlet=0, nextd=1, gpml_sch=0 if kind.endswith("fang") else 1, seed=3)
+    else:
+        m = models.box(mn, aniso=kind.endswith("aniso"), seed=4)
+    w = 2 * math.pi * np.array([0.5, 3.0])
+    p = _problem(m)
+    p.assemble(w, ifreq0=0)
+    o = oracle.Oracle(m)
+    ne = m.ne
+    for f in range(2):
+        K, Mm, b = p.element_matrices(0, ne, f)
+        for e in range(ne):
+            Kr, Mr, br, _ = o.element(e, w[f], ifreq=f)
+            assert _rel(K[e], Kr) < 1e-10, (e, f)
+            assert _rel(Mm[e], Mr) < 1e-10, (e, f)
+            assert _rel(b[e], br) < 1e-10, (e, f)
+
+
+@pytest.mark.parametrize("mn", ORDERS)
+@pytest.mark.parametrize("dirichlet", [1, 0])
+def test_assembled_system(mn, dirichlet):
+    m = models.box(mn, n=(3, 3, 2), dirichlet=dirichlet, nextd=0 if dirichlet else 1, seed=5)
+    w = 2 * math.pi * np.array([0.5, 3.0])
+    p = _problem(m)
+    p.assemble(w)
+    o = oracle.Oracle(m)
+    for f in range(2):
+        ia, ja, a = p.export_coo(f)
+        ra, rrhs = o.assemble(w[f], ifreq=f)
+        ria, rja = o.coo_coords()
+        low = ria >= rja
+        order = np.lexsort((rja[low], ria[low]))
+        ref = ra[low][order]
+        assert np.array_equal(ia, ria[low][order]) and np.array_equal(ja, rja[low][order])
+        assert _rel(a, ref) < 1e-10
+        assert _rel(p.export_rhs(f), rrhs) < 1e-10
+
+
+@pytest.mark.parametrize("mn", ORDERS)
+def test_spmv_matches_cpu_product(mn):
+    m = models.box(mn, n=(3, 3, 2), seed=6)
+    w = 2 * math.pi * 0.5
+    p = _problem(m)
+    p.assemble([w])
+    A, _ = oracle.Oracle(m).matrix(w)
+    rng = np.random.Generator(np.random.PCG64(7))
+    x = rng.normal(size=(2, p.nne)) + 1j * rng.normal(size=(2, p.nne))
+    y = p.spmv(0, x)
+    ref = np.stack([A @ x[0], A @ x[1]])
+    assert _rel(y, ref) < 1e-12
+
+
+def _c1_small():
+    return M.plain_linear_block(ncells=8, d=250.0, n_air=4, dz_air=500.0, nrx=3)
+
+
+@pytest.mark.parametrize("mode", [api.MODE_MIXED, api.MODE_FP64])
+def test_solve_and_impedance_linear(mode):
+    m = _c1_small()
+    w = 2 * math.pi * 1.0
+    o = oracle.Oracle(m)
+    xd, A, rhs = o.solve_direct(w)
+    Zd = o.receivers(w, xd)[2]
+    p = _problem(m)
+    p.assemble([w])
+    x, st = p.solve(tol=1e-10, mode=mode, max_iters=4000)
+    assert st["rel_residual"] <= 1e-10
+    res = max(np.linalg.norm(rhs[k] - A @ x[0, k]) / np.linalg.norm(rhs[k]) for k in range(2))
+    assert res <= 1e-9
+    Z, rho, phi = p.impedance()
+    err = np.linalg.norm(Z[0] - Zd, axis=1) / np.linalg.norm(Zd, axis=1)
+    assert err.max() <= 1e-6
+
+
+def test_impedance_kernel_matches_oracle_on_same_solution():
+    # E, H, Z, rho, phi evaluated in FP64 on the GPU from the GPU solution and by the
+    # oracle from the same solution vector
+    m = _c1_small()
+    w = 2 * math.pi * 1.0
+    p = _problem(m)
+    p.assemble([w])
+    x, _ = p.solve(tol=1e-10)
+    Z, rho, phi, E, H = p.impedance(with_fields=True)
+    Er, Hr, Zr, rhor, phir = oracle.Oracle(m).receivers(w, x[0])
+    assert _rel(E[0], Er) < 1e-11
+    assert _rel(H[0], Hr) < 1e-11
+    assert _rel(Z[0], Zr) < 1e-11
+    assert np.allclose(rho[0], rhor, rtol=1e-11, atol=0)
+    assert np.allclose(phi[0], phir, rtol=1e-11, atol=1e-12)
+
+
+def test_multi_frequency_batch_matches_single():
+    m = _c1_small()
+    w = 2 * math.pi * np.array([0.1, 1.0, 10.0])
+    sig = np.stack([m.sigma_at(x) for x in w])
+    p = _problem(m)
+    p.assemble(w, sigma_f=sig)
+    xb, st = p.solve(tol=1e-10)
+    o = oracle.Oracle(m)
+    for f in range(3):
+        o.set_sigma(sig[f])
+        xd, A, rhs = o.solve_direct(w[f], ifreq=f)
+        assert _rel(p.export_rhs(f), rhs) < 1e-10
+        res = max(np.linalg.norm(rhs[k] - A @ xb[f, k]) / np.linalg.norm(rhs[k]) for k in range(2))
+        assert res <= 1e-9
+
+
+def test_errors_are_reported():
+    m = _c1_small()
+    m.mu[5] = 0.0
+    with pytest.raises(api.MVFError) as e:
+        _problem(m)
+    assert e.value.code == api.E_SINGULAR
+    m = _c1_small()
+    p = _problem(m)
+    with pytest.raises(api.MVFError) as e:
+        p.solve()
+    assert e.value.code == api.E_STATE or isinstance(e.value, api.MVFError)
