@@ -134,6 +134,13 @@ int mvf_impedance(mvf_ctx *ctx, int32_t nrx, const double *xr, const double *yr,
 /* Parity hook: y = A_f x for frequency f in FP64 (x, y: [2][nne] complex, host). */
 int mvf_spmv(mvf_ctx *ctx, int32_t f, const double *x, double *y);
 
+/* Measurement hooks (no reference counterpart): average device time of the FP32
+ * K/M SpMM over all right-hand sides sharing frequency f's matrix, timed with CUDA
+ * events on the library's stream, and its algorithmic bytes per launch; and the
+ * number of kernels this library has launched in the process so far. */
+int mvf_profile_spmm(mvf_ctx *ctx, int32_t f, int32_t reps, double *sec_per_launch, int64_t *bytes);
+int64_t mvf_kernel_launches(void);
+
 #ifdef __cplusplus
 }
 #endif

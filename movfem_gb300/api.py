@@ -53,7 +53,12 @@ class Stats(ctypes.Structure):
 
 EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numbering", "mvf_set_sigma",
            "mvf_assemble", "mvf_export_coo", "mvf_export_rhs", "mvf_element_matrices", "mvf_solve",
-           "mvf_impedance", "mvf_spmv"]
+           "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches"]
+
+
+def kernel_launches() -> int:
+    """Kernels launched by the library in this process so far."""
+    return int(load().mvf_kernel_launches())
 
 _lib = None
 
@@ -88,8 +93,11 @@ def load(build: bool = True):
     L.mvf_solve.argtypes = [P, P, D, I32, I32, P]
     L.mvf_impedance.argtypes = [P, I32, P, P, P, P, P, P, P]
     L.mvf_spmv.argtypes = [P, I32, P, P]
+    L.mvf_profile_spmm.argtypes = [P, I32, I32, P, P]
+    L.mvf_kernel_launches.argtypes = []
+    L.mvf_kernel_launches.restype = I64
     for n in EXPORTS:
-        if n not in ("mvf_destroy", "mvf_last_error", "mvf_create"):
+        if n not in ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches"):
             getattr(L, n).restype = ctypes.c_int
     _lib = L
     return L
@@ -198,6 +206,23 @@ class MTProblem:
         if not (rc == E_NOCONV and not raise_noconv):
             self._chk(rc)
         return buf, st.as_dict()
+
+    def solve_device(self, tol: float = 1e-10, mode: int = MODE_MIXED, max_iters: int = 5000):
+        """Solve with the assembled right-hand sides; the solutions stay on the device
+        (read them through :meth:`impedance`).  Returns the statistics."""
+        st = Stats()
+        rc = self.L.mvf_solve(self.h, None, tol, mode, max_iters, ctypes.byref(st))
+        if rc not in (0, E_NOCONV):
+            self._chk(rc)
+        d = st.as_dict()
+        d["converged"] = rc == 0
+        return d
+
+    def profile_spmm(self, f: int = 0, reps: int = 20):
+        s = ctypes.c_double()
+        b = ctypes.c_int64()
+        self._chk(self.L.mvf_profile_spmm(self.h, f, reps, ctypes.byref(s), ctypes.byref(b)))
+        return {"seconds_per_launch": s.value, "bytes_per_launch": b.value}
 
     def impedance(self, rx=None, with_fields: bool = False):
         rx = self.mesh.rx if rx is None else np.asarray(rx, dtype=np.float64)

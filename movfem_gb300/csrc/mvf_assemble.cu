@@ -320,11 +320,6 @@ __global__ void __launch_bounds__(256) element_kernel(
                         for (int b = 0; b < 3; ++b) S.dk[gl][a][b] = w * mf1[pk(a, b)];
                 }
                 // source for every rhs frequency and both polarisations (p_source)
-                double gradN[MN][3];
-                for (int l = 0; l < MN; ++l) {
-                    const double *d = tdN + (g * MN + l) * 3;
-                    for (int a = 0; a < 3; ++a) gradN[l][a] = ji[a * 3 + 0] * d[0] + ji[a * 3 + 1] * d[1] + ji[a * 3 + 2] * d[2];
-                }
                 for (int f = 0; f < nf; ++f) {
                     const double om = c_ap.omega[f];
                     const double weps = rr32(om * EPS0_D);
@@ -346,9 +341,15 @@ __global__ void __launch_bounds__(256) element_kernel(
                                 dm3[a].im += nv * t.im;
                             }
                             const double *vv = S.v[l][p];
-                            pc[0] += vv[2] * gradN[l][1] - vv[1] * gradN[l][2];
-                            pc[1] += vv[0] * gradN[l][2] - vv[2] * gradN[l][0];
-                            pc[2] += vv[1] * gradN[l][0] - vv[0] * gradN[l][1];
+                            if (vv[0] != 0.0 || vv[1] != 0.0 || vv[2] != 0.0) {
+                                // grad N_l x v (p_pcurl); zero when mu = mu0
+                                const double *d = tdN + (g * MN + l) * 3;
+                                double gn[3];
+                                for (int a = 0; a < 3; ++a) gn[a] = ji[a * 3 + 0] * d[0] + ji[a * 3 + 1] * d[1] + ji[a * 3 + 2] * d[2];
+                                pc[0] += vv[2] * gn[1] - vv[1] * gn[2];
+                                pc[1] += vv[0] * gn[2] - vv[2] * gn[0];
+                                pc[2] += vv[1] * gn[0] - vv[0] * gn[1];
+                            }
                         }
                         const cd wH = cscale(H, w);
                         for (int a = 0; a < 3; ++a) {
@@ -540,6 +541,7 @@ static int launch_elements(Ctx *c, MatrixSet &S, const int32_t *elems, int64_t n
     MVF_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (n <= 0) return 0;
     const int64_t grid = std::min<int64_t>(n, 152 * 16);
+    count_launch();
     kern<<<(unsigned)grid, 256, smem, c->stream>>>(
         elems, n, c->d.xp, c->d.yp, c->d.zp, c->d.sigma, c->d.sigma_f, c->d.mu, c->d.gne, c->d.N, c->d.dN, c->d.L,
         c->d.dL, c->d.gp, c->d.edge_node, c->d.edge_dir, c->d.rowptr, c->d.col, S.K64, S.M64, c->d.rhs, c->nne,
@@ -671,7 +673,9 @@ int assemble_set(Ctx *c, MatrixSet &S, bool gpml, int fset) {
     }
     c->d.rhs = rhs_save;
     if (rc) { cudaFree(errflag); return rc; }
+    count_launch();
     to_f32<<<1024, 256, 0, c->stream>>>(S.K64, S.K32, nnz);
+    count_launch();
     to_f32<<<1024, 256, 0, c->stream>>>(S.M64, S.M32, nnz);
     int herr = 0;
     MVF_CUDA(c, cudaMemcpyAsync(&herr, errflag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));

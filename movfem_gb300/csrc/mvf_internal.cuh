@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -97,6 +98,13 @@ struct Ctx {
     bool keep_elements = false;
     int64_t ke_count = 0;
 };
+
+// process-wide count of the library's kernel launches
+inline std::atomic<int64_t> &launch_counter() {
+    static std::atomic<int64_t> n{0};
+    return n;
+}
+inline void count_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
 
 int fail(Ctx *c, int code, const std::string &msg);
 int cuda_fail(Ctx *c, cudaError_t e, const char *what);

@@ -126,6 +126,8 @@ __global__ void receivers_kernel(const double *__restrict__ xp, const double *__
     const int nord = c_pp.nord, mn = c_pp.mn;
     __shared__ double2 En[4][MVF_MAX_NODES][2][3];  // E at the nodes of each corner's visiting element
     __shared__ double2 Hc[4][2][3], Ec[4][2][3];
+    __shared__ double XcS[4][MVF_MAX_NODES][3];  // element of each corner (kept off the thread stack)
+    __shared__ int64_t idS[4][MVF_MAX_NODES];
     // corner c = a + 2b: top face of element (ie, je, ke)
     for (int t = threadIdx.x; t < 4 * mn; t += blockDim.x) {
         const int c = t / mn, l = t % mn;
@@ -153,8 +155,8 @@ __global__ void receivers_kernel(const double *__restrict__ xp, const double *__
         const int64_t J = (int64_t)je * (nord - 1) + b * (nord - 1);
         const int64_t K = (int64_t)ke * (nord - 1) + (nord - 1);
         const int fi = first_elem(I, c_pp.nx), fj = first_elem(J, c_pp.ny), fk = first_elem(K, c_pp.nz);
-        double X[MVF_MAX_NODES][3];
-        int64_t ids[MVF_MAX_NODES];
+        double(&X)[MVF_MAX_NODES][3] = XcS[c];
+        int64_t(&ids)[MVF_MAX_NODES] = idS[c];
         elem_coords(xp, yp, zp, fi, fj, fk, X, ids);
         const double r[3] = {-1.0 + 2.0 * (double)(I - (int64_t)fi * (nord - 1)) / (nord - 1),
                              -1.0 + 2.0 * (double)(J - (int64_t)fj * (nord - 1)) / (nord - 1),
@@ -303,6 +305,7 @@ extern "C" int mvf_impedance(mvf_ctx *xc, int32_t nrx, const double *xr, const d
     if (H) MVF_CUDA(c, cudaMalloc((void **)&d_H, (size_t)nout * 6 * sizeof(double2)));
     MVF_CUDA(c, cudaMemcpyAsync(d_re, re.data(), re.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     MVF_CUDA(c, cudaMemcpyAsync(d_rxy, rxy.data(), rxy.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    count_launch();
     receivers_kernel<<<nout, 128, 0, c->stream>>>(c->d.xp, c->d.yp, c->d.zp, c->d.mu, c->d.gne, c->d.edge_node,
                                                    c->d.edge_dir, (const double2 *)c->d.x, nrx, d_re, d_rxy, d_Z,
                                                    d_rho, d_phi, d_E, d_H);

@@ -384,6 +384,13 @@ static int create(Ctx *c, const mvf_mesh *m, int device) {
     if (ndev < 1) return fail(c, MVF_E_CUDA, "no CUDA device");
     if (device >= 0) MVF_CUDA(c, cudaSetDevice(device));
     MVF_CUDA(c, cudaGetDevice(&c->device));
+    {
+        // the element and receiver kernels keep per-thread tables on the stack: make
+        // sure the per-thread stack covers them (the default is 1 KB)
+        size_t stack = 0;
+        MVF_CUDA(c, cudaDeviceGetLimit(&stack, cudaLimitStackSize));
+        if (stack < 4096) MVF_CUDA(c, cudaDeviceSetLimit(cudaLimitStackSize, 4096));
+    }
     MVF_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     build_tables(m->nodes_per_elem, m->quirks, c->T);
     const int nord = c->T.nord;

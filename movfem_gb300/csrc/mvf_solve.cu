@@ -398,20 +398,23 @@ __global__ void cast_vec(int64_t n, const double2 *__restrict__ a, TV *__restric
 }
 
 // gather rhs [f][p][n] -> [n][R] and scatter back
-__global__ void gather_rhs(int32_t n, int R, int f0, const double2 *__restrict__ src, double2 *__restrict__ dst) {
+// (padding right-hand sides r >= Rreal read as zero and are not written back)
+__global__ void gather_rhs(int32_t n, int R, int Rreal, int f0, const double2 *__restrict__ src,
+                           double2 *__restrict__ dst) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)n * R;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int r = (int)(q % R);
         const int64_t i = q / R;
-        dst[q] = src[((int64_t)(f0 * 2 + r)) * n + i];
+        dst[q] = r < Rreal ? src[((int64_t)(f0 * 2 + r)) * n + i] : make_double2(0.0, 0.0);
     }
 }
-__global__ void scatter_sol(int32_t n, int R, int f0, const double2 *__restrict__ src, double2 *__restrict__ dst) {
+__global__ void scatter_sol(int32_t n, int R, int Rreal, int f0, const double2 *__restrict__ src,
+                            double2 *__restrict__ dst) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)n * R;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int r = (int)(q % R);
         const int64_t i = q / R;
-        dst[((int64_t)(f0 * 2 + r)) * n + i] = src[q];
+        if (r < Rreal) dst[((int64_t)(f0 * 2 + r)) * n + i] = src[q];
     }
 }
 
@@ -469,6 +472,7 @@ template <class T, class TV>
 static void launch_spmm(Ctx *c, int R, const T *K, const T *M, const TV *x, const TV *b, TV *y, int use_w32) {
     const int threads = 256;
     const int64_t rows_per_block = threads / 32;
+    count_launch();
     const unsigned grid = (unsigned)std::min<int64_t>((c->nne + rows_per_block - 1) / rows_per_block, 152 * 64);
     switch (R) {
         case 1: spmm_km<T, TV, 1><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
@@ -492,15 +496,21 @@ static int cgs2(Ctx *c, Work &W, int k) {
     const int64_t vs = (int64_t)W.n * R;
     for (int pass = 0; pass < 2; ++pass) {
         const size_t sm = (size_t)k * R * sizeof(double2);
+        count_launch();
         multidot<TV><<<W.nblocks, 256, sm, c->stream>>>(W.n, R, k, V, vs, w, W.partial);
+        count_launch();
         reduce_partials<<<k * R, 256, 0, c->stream>>>(W.nblocks, k * R, W.partial, pass == 0 ? W.hc : W.htmp, 0);
+        count_launch();
         axpy_multi<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, k, V, vs, pass == 0 ? W.hc : W.htmp, w);
         if (pass == 1) {
             // hc += htmp
+            count_launch();
             reduce_partials<<<k * R, 256, 0, c->stream>>>(1, k * R, W.htmp, W.hc, 1);
         }
     }
+    count_launch();
     multidot<TV><<<W.nblocks, 256, (size_t)R * sizeof(double2), c->stream>>>(W.n, R, 1, w, vs, w, W.partial);
+    count_launch();
     reduce_partials<<<R, 256, 0, c->stream>>>(W.nblocks, R, W.partial, W.nrm, 0);
     MVF_CUDA(c, cudaGetLastError());
     return 0;
@@ -509,8 +519,10 @@ static int cgs2(Ctx *c, Work &W, int k) {
 template <class TV>
 static void precondition(Ctx *c, Work &W, const TV *r, TV *z) {
     const int R = W.R;
+    count_launch();
     grad_t<TV><<<grid_for((int64_t)c->ngn * R), 256, 0, c->stream>>>(c->ngn, R, c->d.gtrow, c->d.gtcol, c->d.gtval, r,
                                                                     W.pinv, (TV *)W.t);
+    count_launch();
     apply_prec<TV><<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, c->d.grow, c->d.gcol, c->d.gval, r,
                                                                      W.dinv, (const TV *)W.t, z);
 }
@@ -529,9 +541,13 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
     const int use_w32 = 1;
     // V0 = rhs / ||rhs||
     MVF_CUDA(c, cudaMemcpyAsync(w, rhs, W.vb, cudaMemcpyDeviceToDevice, c->stream));
+    count_launch();
     multidot<TV><<<W.nblocks, 256, (size_t)R * sizeof(double2), c->stream>>>(W.n, R, 1, w, vs, w, W.partial);
+    count_launch();
     reduce_partials<<<R, 256, 0, c->stream>>>(W.nblocks, R, W.partial, W.nrm, 0);
+    count_launch();
     hessenberg_init<<<1, 32, 0, c->stream>>>(R, W.nrm, W.hs);
+    count_launch();
     scale_into<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, w, W.nrm, V);
     std::vector<Hess> hh(R);
     std::vector<double> beta(R);
@@ -541,7 +557,9 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
         launch_spmm<T, TV>(c, R, K, M, Z + k * vs, (const TV *)nullptr, w, use_w32);
         int rc = cgs2<TV>(c, W, k + 1);
         if (rc) return rc;
+        count_launch();
         hessenberg_step<<<1, 32, 0, c->stream>>>(R, k, W.hc, W.nrm, W.hs);
+        count_launch();
         scale_into<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, w, W.nrm, V + (k + 1) * vs);
         // check the residual estimate every 10 iterations and at the end
         if ((k + 1) % 10 == 0 || k + 1 == m) {
@@ -556,7 +574,9 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
             if (all) { ++k; break; }
         }
     }
+    count_launch();
     hessenberg_solve<<<1, 32, 0, c->stream>>>(R, k, W.hs, W.y);
+    count_launch();
     update_x<TV, double2><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, k, Z, vs, W.y, x, R, 0);
     MVF_CUDA(c, cudaGetLastError());
     iters += k;
@@ -567,7 +587,9 @@ static int residual_norms(Ctx *c, Work &W, const MatrixSet &S, std::vector<doubl
     const int R = W.R;
     const int64_t vs = (int64_t)W.n * R;
     launch_spmm<double, double2>(c, R, S.K64, S.M64, W.x64, W.b64, W.r64, 1);
+    count_launch();
     multidot<double2><<<W.nblocks, 256, (size_t)R * sizeof(double2), c->stream>>>(W.n, R, 1, W.r64, vs, W.r64, W.partial);
+    count_launch();
     reduce_partials<<<R, 256, 0, c->stream>>>(W.nblocks, R, W.partial, W.nrm, 0);
     std::vector<double2> h(R);
     MVF_CUDA(c, cudaMemcpyAsync(h.data(), W.nrm, R * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
@@ -581,23 +603,30 @@ template <class T>
 static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int npol, double tol, int max_iters,
                      mvf_stats *st, int m) {
     using TV = typename C2<T>::V;
-    const int R = nfs * npol;
+    // the kernels map right-hand sides onto warp lanes: pad to a power of two with
+    // zero right-hand sides (their Krylov sequences stay zero)
+    const int Rreal = nfs * npol;
+    int R = 1;
+    while (R < Rreal) R <<= 1;
     Work W;
     int rc = alloc_work<T>(c, W, R, m);
     if (rc) { free_work(W); return rc; }
     SolveParams sp{};
     for (int r = 0; r < R; ++r) {
-        const int f = f0 + r / npol;
+        const int f = f0 + std::min(r, Rreal - 1) / npol;
         sp.omega[r] = c->omega[f];
         sp.w32[r] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
     }
     MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    count_launch();
     extract_diag<<<grid_for(c->nne), 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.K64, S.M64, W.kd, W.md);
+    count_launch();
     build_inverse_diag<<<grid_for(((int64_t)c->nne + c->ngn) * R), 256, 0, c->stream>>>(
         c->nne, c->ngn, R, W.kd, W.md, S.kphi, S.mphi, S.mabs, W.dinv, W.pinv);
     // gather right-hand sides [f][p][n] -> [n][R]
     if (npol == 2) {
-        gather_rhs<<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, f0, (const double2 *)c->d.rhs, W.b64);
+        count_launch();
+        gather_rhs<<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, Rreal, f0, (const double2 *)c->d.rhs, W.b64);
     } else {
         // single rhs (f0, pol0)
         MVF_CUDA(c, cudaMemcpyAsync(W.b64, (const double2 *)c->d.rhs + ((int64_t)f0 * 2 + pol0) * W.n,
@@ -607,7 +636,9 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
     std::vector<double> bn(R, 1.0), rel(R, 0.0), est(R, 0.0);
     {
         const int64_t vs = (int64_t)W.n * R;
+        count_launch();
         multidot<double2><<<W.nblocks, 256, (size_t)R * sizeof(double2), c->stream>>>(W.n, R, 1, W.b64, vs, W.b64, W.partial);
+        count_launch();
         reduce_partials<<<R, 256, 0, c->stream>>>(W.nblocks, R, W.partial, W.nrm, 0);
         std::vector<double2> h(R);
         MVF_CUDA(c, cudaMemcpyAsync(h.data(), W.nrm, R * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
@@ -620,12 +651,13 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
     while (true) {
         if ((rc = residual_norms(c, W, S, rel, bn))) break;
         worst = 0;
-        for (int r = 0; r < R; ++r) worst = std::max(worst, rel[r]);
+        for (int r = 0; r < Rreal; ++r) worst = std::max(worst, rel[r]);
         if (worst <= tol || iters >= max_iters) break;
         ++outer;
         // inner solve on the scaled residual in the Krylov precision
         TV *rk = (TV *)W.w;  // reuse: cycle copies rhs into w first, so stage in V_m
         TV *stage = (TV *)W.V + (int64_t)W.m * W.n * R;
+        count_launch();
         cast_vec<TV><<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>((int64_t)W.n * R, W.r64, stage, 1.0);
         (void)rk;
         // the cycle writes V_0 from its rhs before V_m is reused, so the staging copy
@@ -634,9 +666,10 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         if ((rc = fgmres_cycle<T>(c, W, S, stage, W.x64, inner_tol, iters, est))) break;
     }
     if (!rc) {
-        if (npol == 2)
-            scatter_sol<<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, f0, W.x64, (double2 *)c->d.x);
-        else
+        if (npol == 2) {
+            count_launch();
+            scatter_sol<<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, Rreal, f0, W.x64, (double2 *)c->d.x);
+        } else
             MVF_CUDA(c, cudaMemcpyAsync((double2 *)c->d.x + ((int64_t)f0 * 2 + pol0) * W.n, W.x64,
                                         (size_t)W.n * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
         MVF_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -697,6 +730,52 @@ extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mod
     return 0;
 }
 
+extern "C" int64_t mvf_kernel_launches(void) { return launch_counter().load(); }
+
+extern "C" int mvf_profile_spmm(mvf_ctx *xc, int32_t f, int32_t reps, double *sec_per_launch, int64_t *bytes) {
+    if (!xc || !sec_per_launch || reps < 1) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
+    if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
+    const MatrixSet *S = nullptr;
+    for (const MatrixSet &s : c->sets)
+        if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
+    int R = 1;
+    while (R < 2 * S->nfreq) R <<= 1;
+    SolveParams sp{};
+    for (int r = 0; r < R; ++r) {
+        const int ff = S->first_freq + std::min(r, 2 * S->nfreq - 1) / 2;
+        sp.omega[r] = c->omega[ff];
+        sp.w32[r] = (double)(float)c->omega[ff];
+    }
+    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    float2 *x, *y;
+    const size_t nb = (size_t)c->nne * R * sizeof(float2);
+    MVF_CUDA(c, cudaMalloc((void **)&x, nb));
+    MVF_CUDA(c, cudaMalloc((void **)&y, nb));
+    MVF_CUDA(c, cudaMemsetAsync(x, 0, nb, c->stream));
+    launch_spmm<float, float2>(c, R, S->K32, S->M32, x, (const float2 *)nullptr, y, 1);  // warm
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->stream);
+    for (int i = 0; i < reps; ++i) launch_spmm<float, float2>(c, R, S->K32, S->M32, x, (const float2 *)nullptr, y, 1);
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(x);
+    cudaFree(y);
+    MVF_CUDA(c, cudaGetLastError());
+    *sec_per_launch = ms * 1e-3 / reps;
+    // algorithmic bytes: K, M (FP32) and column index per nonzero, row pointers (int64),
+    // x gathered once and y written once per right-hand side (complex64)
+    if (bytes) *bytes = c->nnz * 12 + 8 * ((int64_t)c->nne + 1) + 2 * (int64_t)R * c->nne * 8;
+    return 0;
+}
+
 extern "C" int mvf_spmv(mvf_ctx *xc, int32_t f, const double *x, double *y) {
     if (!xc || !x || !y) return MVF_E_ARG;
     Ctx *c = &xc->c;
@@ -716,9 +795,11 @@ extern "C" int mvf_spmv(mvf_ctx *xc, int32_t f, const double *x, double *y) {
     MVF_CUDA(c, cudaMalloc((void **)&tx, nb));
     MVF_CUDA(c, cudaMalloc((void **)&ty, nb));
     MVF_CUDA(c, cudaMemcpyAsync(dx, x, nb, cudaMemcpyHostToDevice, c->stream));
-    gather_rhs<<<grid_for((int64_t)c->nne * 2), 256, 0, c->stream>>>(c->nne, 2, 0, dx, tx);
+    count_launch();
+    gather_rhs<<<grid_for((int64_t)c->nne * 2), 256, 0, c->stream>>>(c->nne, 2, 2, 0, dx, tx);
     launch_spmm<double, double2>(c, 2, S->K64, S->M64, tx, (const double2 *)nullptr, ty, 1);
-    scatter_sol<<<grid_for((int64_t)c->nne * 2), 256, 0, c->stream>>>(c->nne, 2, 0, ty, dy);
+    count_launch();
+    scatter_sol<<<grid_for((int64_t)c->nne * 2), 256, 0, c->stream>>>(c->nne, 2, 2, 0, ty, dy);
     MVF_CUDA(c, cudaMemcpyAsync(y, dy, nb, cudaMemcpyDeviceToHost, c->stream));
     MVF_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(dx); cudaFree(dy); cudaFree(tx); cudaFree(ty);
