@@ -141,6 +141,16 @@ int mvf_spmv(mvf_ctx *ctx, int32_t f, const double *x, double *y);
 int mvf_profile_spmm(mvf_ctx *ctx, int32_t f, int32_t reps, double *sec_per_launch, int64_t *bytes);
 int64_t mvf_kernel_launches(void);
 
+/* y = A_f x like mvf_spmv, for callers that cannot let the library allocate device
+ * memory (a host whose device memory is owned by its own pool, or code between
+ * captured / latency-critical stream steps).  No counterpart in the reference.
+ * x, y: DEVICE pointers, [2][nne] complex.  Nothing is allocated: the staging lives
+ * in a fixed 16 MiB device array shared by all calls, so nne must be <= 262144
+ * (MVF_E_ARG otherwise) and calls that overlap on the GPU race on it.  The first
+ * call on a device looks up that array's address; make it before any stream capture.
+ * Returns after the result is in y. */
+int mvf_spmv_noalloc(mvf_ctx *ctx, int32_t f, const double *x_dev, double *y_dev);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,7 +53,7 @@ class Stats(ctypes.Structure):
 
 EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numbering", "mvf_set_sigma",
            "mvf_assemble", "mvf_export_coo", "mvf_export_rhs", "mvf_element_matrices", "mvf_solve",
-           "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches"]
+           "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches", "mvf_spmv_noalloc"]
 
 
 def kernel_launches() -> int:
@@ -94,6 +94,7 @@ def load(build: bool = True):
     L.mvf_impedance.argtypes = [P, I32, P, P, P, P, P, P, P]
     L.mvf_spmv.argtypes = [P, I32, P, P]
     L.mvf_profile_spmm.argtypes = [P, I32, I32, P, P]
+    L.mvf_spmv_noalloc.argtypes = [P, I32, P, P]
     L.mvf_kernel_launches.argtypes = []
     L.mvf_kernel_launches.restype = I64
     for n in EXPORTS:
@@ -236,6 +237,11 @@ class MTProblem:
         H = np.empty((nf, nrx, 2, 3), dtype=np.complex128) if with_fields else None
         self._chk(self.L.mvf_impedance(self.h, nrx, _p(xr), _p(yr), _p(Z), _p(rho), _p(phi), _p(E), _p(H)))
         return (Z, rho, phi, E, H) if with_fields else (Z, rho, phi)
+
+    def spmv_noalloc(self, f: int, x_dev_ptr: int, y_dev_ptr: int):
+        """y = A_f x on device buffers ([2][nne] complex128) without any allocation
+        by the library; see mvf_spmv_noalloc in include/movfem_gpu.h."""
+        self._chk(self.L.mvf_spmv_noalloc(self.h, f, ctypes.c_void_p(x_dev_ptr), ctypes.c_void_p(y_dev_ptr)))
 
     def spmv(self, f: int, x):
         xx = np.ascontiguousarray(x, dtype=np.complex128).reshape(2, self.nne)

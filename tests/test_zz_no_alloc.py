@@ -1,0 +1,56 @@
+"""mvf_spmv_noalloc: the matrix-vector product for callers that cannot let the
+library allocate device memory (their device memory belongs to their own pool, or
+the call sits between captured / latency-critical stream steps).
+
+It must give the same product as mvf_spmv (the allocating entry point) within the
+tolerance of the SpMV parity test, on two calls in a row -- the second call reuses
+the shared fixed-size staging array left behind by the first.  This file is
+collected last so that a failure here leaves the rest of the suite already run; it
+also passes on its own in a fresh process.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from movfem_gb300 import api
+from movfem_gb300 import mesh as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def test_noalloc_spmv_matches_spmv_twice():
+    torch = pytest.importorskip("torch")
+    m = M.plain_linear_block(ncells=8, d=250.0, n_air=4, dz_air=500.0, nrx=2)
+    w = 2 * math.pi * np.array([0.5, 4.0])
+    p = api.MTProblem(m, device=0)
+    p.assemble(w)
+    rng = np.random.Generator(np.random.PCG64(11))
+    for call, f in enumerate([1, 0]):
+        x = rng.normal(size=(2, p.nne)) + 1j * rng.normal(size=(2, p.nne))
+        ref = p.spmv(f, x)
+        xd = torch.from_numpy(x).to("cuda:0")
+        yd = torch.full((2, p.nne), complex(float("nan"), float("nan")), dtype=torch.complex128, device="cuda:0")
+        torch.cuda.synchronize()
+        p.spmv_noalloc(f, xd.data_ptr(), yd.data_ptr())
+        y = yd.cpu().numpy()
+        assert _rel(y, ref) < 1e-12, f"call {call}"
+
+
+def test_noalloc_rejects_models_above_its_limit():
+    torch = pytest.importorskip("torch")
+    # 46^3 earth cells + 10 air layers: about 355,000 free DOFs, above the 262,144 limit
+    m = M.plain_linear_block(ncells=46, d=100.0, n_air=10, dz_air=200.0, nrx=2)
+    p = api.MTProblem(m, device=0)
+    p.assemble([2 * math.pi])
+    assert p.nne > 262144
+    xd = torch.zeros((2, p.nne), dtype=torch.complex128, device="cuda:0")
+    yd = torch.zeros_like(xd)
+    with pytest.raises(api.MVFError) as e:
+        p.spmv_noalloc(0, xd.data_ptr(), yd.data_ptr())
+    assert e.value.code == api.E_ARG
+    assert "262144" in str(e.value)
