@@ -40,6 +40,11 @@ def make_config(name: str):
         m = M.plain_linear_block()
         return m, {"workload": "plain-linear-20x20x20+10air-dirichlet-1f", "elements": "linear-12-edge",
                    "cells": [20, 20, 30], "freqs": 1, "boundary": "dirichlet"}
+    if name == "plain-linear-60-8f":
+        m = M.plain_linear_block(ncells=60, d=100.0 / 3, n_air=20, dz_air=100.0, nrx=11)
+        m.freqs = np.logspace(-1, 2, 8)
+        return m, {"workload": "plain-linear-60x60x60+20air-dirichlet-8f", "elements": "linear-12-edge",
+                   "cells": [60, 60, 80], "freqs": 8, "boundary": "dirichlet"}
     if name == "quadratic-40x40x30-gpml":
         m = M.layered_blocks(20261203, nodes_per_elem=20, ncx=40, ncy=40, ncz=30, d=50.0, nextd=8, n_air=10,
                              dz_air=100.0, nfreq=8, fmin=1e-3, fmax=100.0, nrx=11, gpml_sch=0)

@@ -72,6 +72,8 @@ typedef struct mvf_stats {
     double rel_residual;      /* max over RHS of ||b - A x|| / ||b|| in FP64 */
     double seconds;           /* device time of the solve */
     int64_t bytes_moved;      /* algorithmic HBM bytes of the executed kernels */
+    int32_t stagnated;        /* 1: stopped at a residual floor (<= 1e-5) set by the
+                                 right-hand side's component in the air-gradient kernel */
 } mvf_stats;
 
 typedef struct mvf_ctx mvf_ctx;

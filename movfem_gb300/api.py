@@ -45,7 +45,7 @@ class _Mesh(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("outer_iters", ctypes.c_int32), ("inner_iters", ctypes.c_int32), ("rel_residual", ctypes.c_double),
-                ("seconds", ctypes.c_double), ("bytes_moved", ctypes.c_int64)]
+                ("seconds", ctypes.c_double), ("bytes_moved", ctypes.c_int64), ("stagnated", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

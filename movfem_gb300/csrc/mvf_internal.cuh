@@ -73,6 +73,9 @@ struct Device {
     double *x = nullptr;
     // element matrices of the last assembly, kept for the parity hook
     double *Ke = nullptr, *Me = nullptr, *be = nullptr;
+    // vertex patches (Schwarz preconditioner of the 36/54-DOF elements)
+    int64_t *patch_ptr = nullptr, *patch_ioff = nullptr;
+    int32_t *patch_dof = nullptr;
 };
 
 struct Ctx {
@@ -97,6 +100,11 @@ struct Ctx {
     bool assembled = false, solved = false;
     bool keep_elements = false;
     int64_t ke_count = 0;
+    // vertex patches
+    bool use_patches = false;
+    int64_t npatch = 0, patch_entries = 0;
+    int patch_max = 0;
+    std::vector<int64_t> pcolor_off;
 };
 
 // process-wide count of the library's kernel launches
@@ -123,6 +131,12 @@ void build_tables(int mn, int quirks, OrderTables &T);
 int assemble_set(Ctx *c, MatrixSet &S, bool gpml, int fset);
 int assemble_rhs(Ctx *c);
 void free_sets(Ctx *c);
+
+// vertex-patch Schwarz preconditioner (mvf_patch.cu)
+int patch_setup(Ctx *c);
+int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **inv_out);
+void patch_apply(Ctx *c, const double2 *inv, int R, int npol, int nfi, const float2 *r, float2 *z);
+void patch_apply(Ctx *c, const double2 *inv, int R, int npol, int nfi, const double2 *r, double2 *z);
 
 }  // namespace mvf
 

@@ -1,0 +1,295 @@
+// mvf_patch.cu -- vertex-patch additive Schwarz preconditioner for the 36- and 54-DOF
+// elements.
+//
+// Point Jacobi (with or without a gradient correction) barely reduces the residual
+// of the mixed-order quadratic and Lagrangian edge systems.  The preconditioner here
+// is z = sum_v R_v^T A_v^-1 R_v r over the vertices v of the element grid, where R_v
+// restricts to the DOFs whose elements all lie in the 2x2x2 block of elements around
+// v (the Arnold-Falk-Winther patches for H(curl)); each block contains the local
+// gradient modes, so the curl-curl kernel is handled inside the local solves.
+// A_v depends on the frequency (A = K + i w M): the inverses are formed per frequency
+// by Gauss-Jordan elimination with partial pivoting in FP64 (a relative shift of 1e-10
+// of the largest diagonal entry keeps the patches that lie entirely in the air, where
+// A_v is singular, invertible) and stored in complex FP64: those inverses carry large
+// components along the air gradients, which complex64 cannot hold next to the rest.  Patches of one vertex-parity
+// colour share no DOF, so the 8 colour launches accumulate z without atomics.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <vector>
+
+#include "mvf_internal.cuh"
+
+namespace mvf {
+
+// Build the patch lists (host, once per context).
+int patch_setup(Ctx *c) {
+    const int me = c->T.me;
+    const int nx = c->mesh.nx, ny = c->mesh.ny, nz = c->mesh.nz;
+    const int32_t n = c->nne;
+    std::vector<int32_t> lo(3 * (size_t)n, INT32_MAX), hi(3 * (size_t)n, -1);
+    for (int ie = 0; ie < nx; ++ie)
+        for (int je = 0; je < ny; ++je)
+            for (int ke = 0; ke < nz; ++ke) {
+                const int64_t e = ((int64_t)ie * ny + je) * nz + ke;
+                const int idx[3] = {ie, je, ke};
+                for (int j = 0; j < me; ++j) {
+                    const int32_t g = c->gne_h[(size_t)e * me + j];
+                    if (g <= 0) continue;
+                    for (int a = 0; a < 3; ++a) {
+                        lo[3 * (size_t)(g - 1) + a] = std::min(lo[3 * (size_t)(g - 1) + a], idx[a]);
+                        hi[3 * (size_t)(g - 1) + a] = std::max(hi[3 * (size_t)(g - 1) + a], idx[a]);
+                    }
+                }
+            }
+    // a DOF lies in the patch of vertex v when v-1 <= lo and hi <= v on every axis
+    const int64_t nvx = nx + 1, nvy = ny + 1, nvz = nz + 1, nv = nvx * nvy * nvz;
+    std::vector<int32_t> cnt(nv, 0);
+    auto for_patches = [&](int32_t g, auto &&fn) {
+        int a0[3], a1[3];
+        for (int a = 0; a < 3; ++a) {
+            a0[a] = hi[3 * (size_t)g + a];
+            a1[a] = lo[3 * (size_t)g + a] + 1;
+        }
+        for (int vi = a0[0]; vi <= a1[0]; ++vi)
+            for (int vj = a0[1]; vj <= a1[1]; ++vj)
+                for (int vk = a0[2]; vk <= a1[2]; ++vk) fn(((int64_t)vi * nvy + vj) * nvz + vk);
+    };
+    for (int32_t g = 0; g < n; ++g) for_patches(g, [&](int64_t v) { cnt[v]++; });
+    // order patches by colour (vertex parity), drop empty ones
+    std::vector<int64_t> order;
+    order.reserve(nv);
+    c->pcolor_off.assign(9, 0);
+    for (int col = 0; col < 8; ++col) {
+        c->pcolor_off[col] = (int64_t)order.size();
+        for (int64_t vi = col & 1; vi < nvx; vi += 2)
+            for (int64_t vj = (col >> 1) & 1; vj < nvy; vj += 2)
+                for (int64_t vk = (col >> 2) & 1; vk < nvz; vk += 2) {
+                    const int64_t v = (vi * nvy + vj) * nvz + vk;
+                    if (cnt[v] > 0) order.push_back(v);
+                }
+    }
+    c->pcolor_off[8] = (int64_t)order.size();
+    const int64_t np = (int64_t)order.size();
+    std::vector<int64_t> slot(nv, -1);
+    for (int64_t p = 0; p < np; ++p) slot[order[p]] = p;
+    std::vector<int64_t> ptr(np + 1, 0);
+    for (int64_t p = 0; p < np; ++p) ptr[p + 1] = ptr[p] + cnt[order[p]];
+    std::vector<int32_t> dof(ptr[np]);
+    std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+    for (int32_t g = 0; g < n; ++g) for_patches(g, [&](int64_t v) { dof[fill[slot[v]]++] = g; });
+    int pmax = 0;
+    std::vector<int64_t> ioff(np + 1, 0);
+    for (int64_t p = 0; p < np; ++p) {
+        const int sz = (int)(ptr[p + 1] - ptr[p]);
+        pmax = std::max(pmax, sz);
+        ioff[p + 1] = ioff[p] + (int64_t)sz * sz;
+    }
+    c->npatch = np;
+    c->patch_max = pmax;
+    c->patch_entries = ioff[np];
+    MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_ptr, (np + 1) * sizeof(int64_t)));
+    MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_dof, std::max<int64_t>(ptr[np], 1) * sizeof(int32_t)));
+    MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_ioff, (np + 1) * sizeof(int64_t)));
+    MVF_CUDA(c, cudaMemcpy(c->d.patch_ptr, ptr.data(), (np + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    MVF_CUDA(c, cudaMemcpy(c->d.patch_dof, dof.data(), ptr[np] * sizeof(int32_t), cudaMemcpyHostToDevice));
+    MVF_CUDA(c, cudaMemcpy(c->d.patch_ioff, ioff.data(), (np + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+// Gather A_v = K + i w M over the patch DOFs into ws (complex FP64, P x P row-major),
+// invert it in place by Gauss-Jordan with partial pivoting and store the inverse as
+// complex64.  One CTA per patch (grid-stride); ws is a per-CTA workspace.
+__global__ void __launch_bounds__(256) patch_invert_kernel(
+    int64_t np, const int64_t *__restrict__ pptr, const int32_t *__restrict__ pdof, const int64_t *__restrict__ ioff,
+    const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col, const double *__restrict__ K,
+    const double *__restrict__ M, double w, int pmax, double2 *__restrict__ ws_all, double2 *__restrict__ inv,
+    int *__restrict__ err) {
+    __shared__ int piv_row;
+    __shared__ double red_v[256];
+    __shared__ int red_i[256];
+    double2 *ws = ws_all + (size_t)blockIdx.x * pmax * pmax * 2;  // [P][2P]: A | I
+    for (int64_t p = blockIdx.x; p < np; p += gridDim.x) {
+        const int64_t b0 = pptr[p];
+        const int P = (int)(pptr[p + 1] - b0);
+        const int W2 = 2 * P;
+        // gather
+        for (int t = threadIdx.x; t < P * P; t += blockDim.x) {
+            const int i = t / P, j = t % P;
+            const int32_t gi = pdof[b0 + i], gj = pdof[b0 + j];
+            int64_t lo = rowptr[gi], hi = rowptr[gi + 1] - 1;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (col[mid] < gj) lo = mid + 1;
+                else hi = mid;
+            }
+            double2 a = make_double2(0.0, 0.0);
+            if (col[lo] == gj) a = make_double2(K[lo], w * M[lo]);
+            ws[i * W2 + j] = a;
+            ws[i * W2 + P + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+        }
+        __syncthreads();
+        // shift: 1e-10 of the largest diagonal modulus
+        if (threadIdx.x == 0) {
+            double dmax = 0.0;
+            for (int i = 0; i < P; ++i) dmax = fmax(dmax, hypot(ws[i * W2 + i].x, ws[i * W2 + i].y));
+            const double s = 1e-10 * dmax;
+            for (int i = 0; i < P; ++i) ws[i * W2 + i].x += s;
+        }
+        __syncthreads();
+        for (int k = 0; k < P; ++k) {
+            // pivot search over rows k..P-1 of column k
+            double best = -1.0;
+            int bi = k;
+            for (int i = k + threadIdx.x; i < P; i += blockDim.x) {
+                const double v = hypot(ws[i * W2 + k].x, ws[i * W2 + k].y);
+                if (v > best) { best = v; bi = i; }
+            }
+            red_v[threadIdx.x] = best;
+            red_i[threadIdx.x] = bi;
+            __syncthreads();
+            for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+                if (threadIdx.x < o && red_v[threadIdx.x + o] > red_v[threadIdx.x]) {
+                    red_v[threadIdx.x] = red_v[threadIdx.x + o];
+                    red_i[threadIdx.x] = red_i[threadIdx.x + o];
+                }
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) {
+                piv_row = red_i[0];
+                if (!(red_v[0] > 0.0)) atomicExch(err, 1);
+            }
+            __syncthreads();
+            const int pr = piv_row;
+            if (pr != k)
+                for (int j = threadIdx.x; j < W2; j += blockDim.x) {
+                    const double2 t = ws[k * W2 + j];
+                    ws[k * W2 + j] = ws[pr * W2 + j];
+                    ws[pr * W2 + j] = t;
+                }
+            __syncthreads();
+            // scale row k by 1/pivot
+            const double2 pv = ws[k * W2 + k];
+            const double s2 = pv.x * pv.x + pv.y * pv.y;
+            const double2 ip = s2 > 0 ? make_double2(pv.x / s2, -pv.y / s2) : make_double2(0.0, 0.0);
+            __syncthreads();
+            for (int j = threadIdx.x; j < W2; j += blockDim.x) {
+                const double2 a = ws[k * W2 + j];
+                ws[k * W2 + j] = make_double2(a.x * ip.x - a.y * ip.y, a.x * ip.y + a.y * ip.x);
+            }
+            __syncthreads();
+            // eliminate column k from every other row
+            for (int t = threadIdx.x; t < P * W2; t += blockDim.x) {
+                const int i = t / W2, j = t % W2;
+                if (i == k || j == k) continue;
+                const double2 f = ws[i * W2 + k];
+                const double2 r = ws[k * W2 + j];
+                ws[i * W2 + j].x -= f.x * r.x - f.y * r.y;
+                ws[i * W2 + j].y -= f.x * r.y + f.y * r.x;
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < P; i += blockDim.x)
+                if (i != k) ws[i * W2 + k] = make_double2(0.0, 0.0);
+            __syncthreads();
+        }
+        double2 *out = inv + ioff[p];
+        for (int t = threadIdx.x; t < P * P; t += blockDim.x) {
+            const int i = t / P, j = t % P;
+            out[t] = ws[i * W2 + P + j];
+        }
+        __syncthreads();
+    }
+}
+
+// z[dof][r] += A_v^-1 r[dof][r] for the patches [p0, p1) (one colour); the inverse of
+// right-hand side r's frequency is inv + (r / npol) * entries.
+template <class TV>
+__global__ void __launch_bounds__(128) patch_apply_kernel(int64_t p0, int64_t p1, const int64_t *__restrict__ pptr,
+                                                          const int32_t *__restrict__ pdof,
+                                                          const int64_t *__restrict__ ioff,
+                                                          const double2 *__restrict__ inv, int64_t fstride, int R,
+                                                          int npol, int nfi, const TV *__restrict__ r,
+                                                          TV *__restrict__ z) {
+    extern __shared__ double2 rs[];  // [P][R]
+    for (int64_t p = p0 + blockIdx.x; p < p1; p += gridDim.x) {
+        const int64_t b0 = pptr[p];
+        const int P = (int)(pptr[p + 1] - b0);
+        for (int t = threadIdx.x; t < P * R; t += blockDim.x) {
+            const int i = t / R, q = t % R;
+            const TV v = r[(int64_t)pdof[b0 + i] * R + q];
+            rs[t] = make_double2(v.x, v.y);
+        }
+        __syncthreads();
+        const double2 *A = inv + ioff[p];
+        for (int t = threadIdx.x; t < P * R; t += blockDim.x) {
+            const int i = t / R, q = t % R;
+            const double2 *Ai = A + (int64_t)min(q / npol, nfi - 1) * fstride + (int64_t)i * P;
+            double sr = 0.0, si = 0.0;
+            for (int j = 0; j < P; ++j) {
+                const double2 a = Ai[j];
+                const double2 x = rs[j * R + q];
+                sr += a.x * x.x - a.y * x.y;
+                si += a.x * x.y + a.y * x.x;
+            }
+            TV &o = z[(int64_t)pdof[b0 + i] * R + q];
+            o.x += (decltype(o.x))sr;
+            o.y += (decltype(o.y))si;
+        }
+        __syncthreads();
+    }
+}
+
+// Inverses for the frequencies w[0..nf) of matrix set S: inv[f][entries].
+int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **inv_out) {
+    double2 *inv = nullptr;
+    const int64_t ent = c->patch_entries;
+    MVF_CUDA(c, cudaMalloc((void **)&inv, std::max<int64_t>(ent * nf, 1) * sizeof(double2)));
+    const int grid = (int)std::min<int64_t>(c->npatch, 152 * 8);
+    double2 *ws = nullptr;
+    int *err = nullptr;
+    MVF_CUDA(c, cudaMalloc((void **)&ws, (size_t)grid * c->patch_max * c->patch_max * 2 * sizeof(double2)));
+    MVF_CUDA(c, cudaMalloc((void **)&err, sizeof(int)));
+    MVF_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+    for (int f = 0; f < nf; ++f) {
+        count_launch();
+        patch_invert_kernel<<<grid, 256, 0, c->stream>>>(c->npatch, c->d.patch_ptr, c->d.patch_dof, c->d.patch_ioff,
+                                                          c->d.rowptr, c->d.col, S.K64, S.M64, w[f], c->patch_max, ws,
+                                                          inv + (int64_t)f * ent, err);
+    }
+    MVF_CUDA(c, cudaGetLastError());
+    int herr = 0;
+    MVF_CUDA(c, cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(ws);
+    cudaFree(err);
+    if (herr) {
+        cudaFree(inv);
+        return fail(c, MVF_E_SINGULAR, "zero pivot in a patch inverse");
+    }
+    *inv_out = inv;
+    return 0;
+}
+
+template <class TV>
+static void apply_impl(Ctx *c, const double2 *inv, int R, int npol, int nfi, const TV *r, TV *z) {
+    cudaMemsetAsync(z, 0, (size_t)c->nne * R * sizeof(TV), c->stream);
+    const size_t sm = (size_t)c->patch_max * R * sizeof(double2);
+    cudaFuncSetAttribute(patch_apply_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    for (int col = 0; col < 8; ++col) {
+        const int64_t a = c->pcolor_off[col], b = c->pcolor_off[col + 1];
+        if (b <= a) continue;
+        const unsigned grid = (unsigned)std::min<int64_t>(b - a, 152 * 16);
+        count_launch();
+        patch_apply_kernel<TV><<<grid, 128, sm, c->stream>>>(a, b, c->d.patch_ptr, c->d.patch_dof, c->d.patch_ioff, inv,
+                                                             c->patch_entries, R, npol, nfi, r, z);
+    }
+}
+
+void patch_apply(Ctx *c, const double2 *inv, int R, int npol, int nfi, const float2 *r, float2 *z) {
+    apply_impl<float2>(c, inv, R, npol, nfi, r, z);
+}
+void patch_apply(Ctx *c, const double2 *inv, int R, int npol, int nfi, const double2 *r, double2 *z) {
+    apply_impl<double2>(c, inv, R, npol, nfi, r, z);
+}
+
+}  // namespace mvf

@@ -456,7 +456,11 @@ static int create(Ctx *c, const mvf_mesh *m, int device) {
         if ((rc = upload(c, &c->d.edge_node, en.data(), en.size()))) return rc;
         if ((rc = upload(c, &c->d.edge_dir, ed.data(), ed.size()))) return rc;
     }
-    return build_gradient(c);
+    if ((rc = build_gradient(c))) return rc;
+    // the 36- and 54-DOF elements are preconditioned with vertex patches
+    c->use_patches = c->T.mn != 8;
+    if (c->use_patches && (rc = patch_setup(c))) return rc;
+    return 0;
 }
 
 static void release(Ctx *c) {
@@ -464,7 +468,8 @@ static void release(Ctx *c) {
     void *ptrs[] = {c->d.xp, c->d.yp, c->d.zp, c->d.sigma, c->d.sigma_f, c->d.mu, c->d.gne, c->d.elem_color,
                     c->d.N, c->d.dN, c->d.L, c->d.dL, c->d.gp, c->d.Gloc, c->d.edge_node, c->d.edge_dir,
                     c->d.rowptr, c->d.col, c->d.grow, c->d.gcol, c->d.gval, c->d.gtrow, c->d.gtcol, c->d.gtval,
-                    c->d.node_gidx, c->d.rhs, c->d.x, c->d.Ke, c->d.Me, c->d.be};
+                    c->d.node_gidx, c->d.rhs, c->d.x, c->d.Ke, c->d.Me, c->d.be, c->d.patch_ptr,
+                    c->d.patch_ioff, c->d.patch_dof};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     c->d = Device{};

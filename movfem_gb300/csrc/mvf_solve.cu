@@ -37,8 +37,11 @@ struct SolveParams {
 };
 __constant__ SolveParams c_sp;
 
-// y = A x (beta = 0) or y = b - A x (sub = 1) for R right-hand sides sharing K, M.
-// One warp per row; lane l handles rhs l % R over the nonzeros k = l / R + s*(32/R).
+// y = A x (b == nullptr) or y = b - A x for R right-hand sides sharing K, M.
+// One warp per row.  The warp loads 32 consecutive nonzeros (K, M, column) with
+// coalesced loads, then broadcasts them by shuffle: lane l works on right-hand side
+// l % R for the nonzeros j = l / R, l / R + 32/R, ... of the chunk, reading
+// x[col][r] as one contiguous run of R complex values per nonzero.
 template <class T, class TV, int R>
 __global__ void __launch_bounds__(256) spmm_km(int32_t n, const int64_t *__restrict__ rowptr,
                                                 const int32_t *__restrict__ col, const T *__restrict__ K,
@@ -52,14 +55,27 @@ __global__ void __launch_bounds__(256) spmm_km(int32_t n, const int64_t *__restr
          row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
         const int64_t k0 = rowptr[row], k1 = rowptr[row + 1];
         T ar = 0, ai = 0, br = 0, bi = 0;
-        for (int64_t k = k0 + s; k < k1; k += SL) {
-            const T kv = K[k], mv = M[k];
-            const TV xv = x[(int64_t)col[k] * R + r];
-            // (K + i w M)(xr + i xi)
-            ar += kv * xv.x;
-            ai += kv * xv.y;
-            br += mv * xv.x;
-            bi += mv * xv.y;
+        for (int64_t kc = k0; kc < k1; kc += 32) {
+            const int cnt = (int)min((int64_t)32, k1 - kc);
+            const bool have = lane < cnt;
+            const T kl = have ? K[kc + lane] : T(0);
+            const T ml = have ? M[kc + lane] : T(0);
+            const int cl = have ? col[kc + lane] : 0;
+#pragma unroll
+            for (int jb = 0; jb < 32; jb += SL) {
+                const int j = jb + s;
+                const T kv = __shfl_sync(0xffffffffu, kl, j);
+                const T mv = __shfl_sync(0xffffffffu, ml, j);
+                const int c = __shfl_sync(0xffffffffu, cl, j);
+                if (j < cnt) {
+                    const TV xv = x[(int64_t)c * R + r];
+                    // (K + i w M)(xr + i xi)
+                    ar += kv * xv.x;
+                    ai += kv * xv.y;
+                    br += mv * xv.x;
+                    bi += mv * xv.y;
+                }
+            }
         }
         T yr = ar - w * bi, yi = ai + w * br;
 #pragma unroll
@@ -421,6 +437,7 @@ __global__ void scatter_sol(int32_t n, int R, int Rreal, int f0, const double2 *
 // ------------------------------------------------------------------------ host side
 struct Work {
     int R = 0, m = 0;
+    int passes = 2;  // Gram-Schmidt passes per iteration
     int32_t n = 0;
     int nblocks = 0;
     void *V = nullptr, *Z = nullptr, *w = nullptr, *t = nullptr;  // Krylov precision
@@ -430,10 +447,13 @@ struct Work {
     double *kd = nullptr, *md = nullptr;
     Hess *hs = nullptr;
     size_t vb = 0;
+    double2 *pinvs = nullptr;  // vertex-patch inverses, one set per frequency
+    int npol = 2, nfi = 1;
 };
 
 static void free_work(Work &W) {
-    void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs};
+    void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs,
+                 W.pinvs};
     for (void *q : p)
         if (q) cudaFree(q);
     W = Work{};
@@ -445,7 +465,8 @@ static int alloc_work(Ctx *c, Work &W, int R, int m) {
     W.R = R;
     W.m = m;
     W.n = c->nne;
-    W.nblocks = 152 * 4;
+    // reduction blocks: about 16 vector entries per thread, at most 4 per SM
+    W.nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(152 * 4, ((int64_t)c->nne * R + 4095) / 4096));
     const size_t nv = (size_t)W.n * R;
     W.vb = nv * sizeof(TV);
     MVF_CUDA(c, cudaMalloc(&W.V, W.vb * (m + 1)));
@@ -486,15 +507,15 @@ static void launch_spmm(Ctx *c, int R, const T *K, const T *M, const TV *x, cons
 
 static unsigned grid_for(int64_t n) { return (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 32); }
 
-// Orthogonalise w against V_0..V_{k-1} (two classical Gram-Schmidt passes), write the
-// projections to W.hc[0..k) and ||w||^2 to W.nrm.
+// Orthogonalise w against V_0..V_{k-1} with W.passes classical Gram-Schmidt passes
+// (FP64 projections), write the projections to W.hc[0..k) and ||w||^2 to W.nrm.
 template <class TV>
 static int cgs2(Ctx *c, Work &W, int k) {
     const int R = W.R;
     const TV *V = (const TV *)W.V;
     TV *w = (TV *)W.w;
     const int64_t vs = (int64_t)W.n * R;
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass < W.passes; ++pass) {
         const size_t sm = (size_t)k * R * sizeof(double2);
         count_launch();
         multidot<TV><<<W.nblocks, 256, sm, c->stream>>>(W.n, R, k, V, vs, w, W.partial);
@@ -519,6 +540,10 @@ static int cgs2(Ctx *c, Work &W, int k) {
 template <class TV>
 static void precondition(Ctx *c, Work &W, const TV *r, TV *z) {
     const int R = W.R;
+    if (W.pinvs) {
+        patch_apply(c, W.pinvs, R, W.npol, W.nfi, r, z);
+        return;
+    }
     count_launch();
     grad_t<TV><<<grid_for((int64_t)c->ngn * R), 256, 0, c->stream>>>(c->ngn, R, c->d.gtrow, c->d.gtcol, c->d.gtval, r,
                                                                     W.pinv, (TV *)W.t);
@@ -611,6 +636,17 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
     Work W;
     int rc = alloc_work<T>(c, W, R, m);
     if (rc) { free_work(W); return rc; }
+    // the FP32 inner solve sits inside FP64 refinement, which absorbs the loss of
+    // orthogonality of a single pass; the plain FP64 method keeps two passes
+    W.passes = std::is_same<T, float>::value ? 1 : 2;
+    W.npol = npol;
+    W.nfi = nfs;
+    if (c->use_patches) {
+        std::vector<double> wl(nfs);
+        for (int f = 0; f < nfs; ++f)
+            wl[f] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f0 + f] : c->omega[f0 + f];
+        if ((rc = patch_invert(c, S, wl.data(), nfs, &W.pinvs))) { free_work(W); return rc; }
+    }
     SolveParams sp{};
     for (int r = 0; r < R; ++r) {
         const int f = f0 + std::min(r, Rreal - 1) / npol;
@@ -648,20 +684,31 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
     int iters = 0, outer = 0;
     const bool mixed = std::is_same<T, float>::value;
     double worst = 1.0;
+    bool stagnated = false;
+    std::vector<double> hist;
     while (true) {
         if ((rc = residual_norms(c, W, S, rel, bn))) break;
         worst = 0;
         for (int r = 0; r < Rreal; ++r) worst = std::max(worst, rel[r]);
+        hist.push_back(worst);
         if (worst <= tol || iters >= max_iters) break;
+        // Residual floor: without a Dirichlet constraint on them, gradients of nodal
+        // functions inside the air (Re(sigma) = 0) are in the kernel of A, and the
+        // right-hand side carries a component there whenever the nodal sigma's
+        // imaginary part differs from i*eps*omega (update_sigma refreshes only part of
+        // the nodes, geometry.f90:144-153).  No solver reduces that component; the rest
+        // of the residual, and the surface fields, converge.  Stop once two refinement
+        // steps have not halved the true residual.
+        if (hist.size() >= 3 && worst > 0.5 * hist[hist.size() - 3] && worst < 1e-5) {
+            stagnated = true;
+            break;
+        }
         ++outer;
-        // inner solve on the scaled residual in the Krylov precision
-        TV *rk = (TV *)W.w;  // reuse: cycle copies rhs into w first, so stage in V_m
+        // inner solve on the residual in the Krylov precision, staged in V_m (the cycle
+        // reads it into V_0 before V_m is overwritten)
         TV *stage = (TV *)W.V + (int64_t)W.m * W.n * R;
         count_launch();
         cast_vec<TV><<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>((int64_t)W.n * R, W.r64, stage, 1.0);
-        (void)rk;
-        // the cycle writes V_0 from its rhs before V_m is reused, so the staging copy
-        // is consumed first
         const double inner_tol = mixed ? std::max(tol / std::max(worst, 1e-300), 2e-5) : tol / std::max(worst, 1e-300);
         if ((rc = fgmres_cycle<T>(c, W, S, stage, W.x64, inner_tol, iters, est))) break;
     }
@@ -678,9 +725,10 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         st->outer_iters = std::max(st->outer_iters, outer);
         st->inner_iters = std::max(st->inner_iters, iters);
         st->rel_residual = std::max(st->rel_residual, worst);
+        if (stagnated) st->stagnated = 1;
     }
     free_work(W);
-    if (!rc && worst > tol) return MVF_E_NOCONV;
+    if (!rc && worst > tol && !stagnated) return MVF_E_NOCONV;
     return rc;
 }
 
@@ -703,8 +751,11 @@ extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mod
     int rc = 0, noconv = 0;
     for (const MatrixSet &S : c->sets) {
         if (mode == 0) {
-            // all frequencies of the set and both polarisations in one batch
-            int r = solve_set<float>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, 40);
+            // all frequencies of the set and both polarisations in one batch; complex
+            // FP32 Krylov vectors, except with the vertex-patch preconditioner of the
+            // 36/54-DOF elements, whose air-patch inverses need FP64 vectors
+            int r = c->use_patches ? solve_set<double>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, 40)
+                                   : solve_set<float>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, 40);
             if (r == MVF_E_NOCONV) noconv = 1;
             else if (r) { rc = r; break; }
         } else {
