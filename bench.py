@@ -147,6 +147,9 @@ def run_ours(args):
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
     m, cfg = make_config(args.config)
+    if args.max_iters is None:
+        args.max_iters = 3000 if m.nodes_per_elem == 8 else 200
+    cfg["max_iters"] = args.max_iters
     omega = 2 * math.pi * m.freqs
     sig_f = np.stack([m.sigma_at(w) for w in omega])
     t0 = time.time()
@@ -285,13 +288,15 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="quadratic-40x40x30-gpml")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--ref-tol", type=float, default=1e-12)
-    ap.add_argument("--max-iters", type=int, default=3000)
+    ap.add_argument("--max-iters", type=int, default=None,
+                    help="Krylov iteration cap (default: 3000 for linear elements, 200 otherwise, so that a "
+                         "default run of the quadratic GPML workload ends within minutes)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

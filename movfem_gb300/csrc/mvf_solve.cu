@@ -98,6 +98,61 @@ __global__ void __launch_bounds__(256) spmm_km(int32_t n, const int64_t *__restr
     }
 }
 
+// Variant for R <= 4 right-hand sides: lanes stride directly over the row's nonzeros
+// (32/R consecutive nonzeros per step, loads coalesced across the lanes of one rhs),
+// two steps in flight per iteration.
+template <class T, class TV, int R>
+__global__ void __launch_bounds__(256) spmm_km_direct(int32_t n, const int64_t *__restrict__ rowptr,
+                                                       const int32_t *__restrict__ col, const T *__restrict__ K,
+                                                       const T *__restrict__ M, const TV *__restrict__ x,
+                                                       const TV *__restrict__ b, TV *__restrict__ y, int use_w32) {
+    constexpr int SL = 32 / R;
+    const int lane = threadIdx.x & 31;
+    const int r = lane % R, s = lane / R;
+    const T w = use_w32 ? (T)c_sp.w32[r] : (T)c_sp.omega[r];
+    for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n;
+         row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int64_t k0 = rowptr[row], k1 = rowptr[row + 1];
+        T ar = 0, ai = 0, br = 0, bi = 0;
+        int64_t k = k0 + s;
+        for (; k + SL < k1; k += 2 * SL) {
+            const T kv0 = __ldg(K + k), mv0 = __ldg(M + k), kv1 = __ldg(K + k + SL), mv1 = __ldg(M + k + SL);
+            const int c0 = __ldg(col + k), c1 = __ldg(col + k + SL);
+            const TV x0 = x[(int64_t)c0 * R + r], x1 = x[(int64_t)c1 * R + r];
+            ar += kv0 * x0.x + kv1 * x1.x;
+            ai += kv0 * x0.y + kv1 * x1.y;
+            br += mv0 * x0.x + mv1 * x1.x;
+            bi += mv0 * x0.y + mv1 * x1.y;
+        }
+        if (k < k1) {
+            const T kv = __ldg(K + k), mv = __ldg(M + k);
+            const TV xv = x[(int64_t)__ldg(col + k) * R + r];
+            ar += kv * xv.x;
+            ai += kv * xv.y;
+            br += mv * xv.x;
+            bi += mv * xv.y;
+        }
+        T yr = ar - w * bi, yi = ai + w * br;
+#pragma unroll
+        for (int o = 16; o >= R; o >>= 1) {
+            yr += __shfl_down_sync(0xffffffffu, yr, o);
+            yi += __shfl_down_sync(0xffffffffu, yi, o);
+        }
+        if (s == 0) {
+            TV out;
+            if (b) {
+                const TV bv = b[row * R + r];
+                out.x = bv.x - yr;
+                out.y = bv.y - yi;
+            } else {
+                out.x = yr;
+                out.y = yi;
+            }
+            y[row * R + r] = out;
+        }
+    }
+}
+
 // diagonal entries of K and M
 __global__ void extract_diag(int32_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
                              const double *__restrict__ K, const double *__restrict__ M, double *__restrict__ kd,
@@ -496,9 +551,9 @@ static void launch_spmm(Ctx *c, int R, const T *K, const T *M, const TV *x, cons
     count_launch();
     const unsigned grid = (unsigned)std::min<int64_t>((c->nne + rows_per_block - 1) / rows_per_block, 152 * 64);
     switch (R) {
-        case 1: spmm_km<T, TV, 1><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
-        case 2: spmm_km<T, TV, 2><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
-        case 4: spmm_km<T, TV, 4><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+        case 1: spmm_km_direct<T, TV, 1><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+        case 2: spmm_km_direct<T, TV, 2><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+        case 4: spmm_km_direct<T, TV, 4><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
         case 8: spmm_km<T, TV, 8><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
         case 16: spmm_km<T, TV, 16><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
         default: spmm_km<T, TV, 32><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
