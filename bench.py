@@ -221,7 +221,8 @@ def run_ours(args):
                      "fp64_plain_solves_per_s": nf / fp64_s if fp64_s > 0 else None},
         "e2e": {"value": e2e_value, "unit": "solves/s",
                 "h2d_bytes_per_step": int(rhs.nbytes), "d2h_bytes_per_step": int(rhs.nbytes)},
-        "roofline": {"bound": "hbm", "kernel": "spmm_km<float>", "achieved": achieved, "peak": hbm,
+        "roofline": {"bound": "hbm", "kernel": "K/M SpMM, FP32, autotuned", "tuning": prob.spmm_tuning(),
+                     "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
                      "bytes_per_launch": spmm_bytes, "us_per_launch": prof["seconds_per_launch"] * 1e6,
                      "traffic": None},

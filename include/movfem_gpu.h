@@ -143,6 +143,22 @@ int mvf_spmv(mvf_ctx *ctx, int32_t f, const double *x, double *y);
 int mvf_profile_spmm(mvf_ctx *ctx, int32_t f, int32_t reps, double *sec_per_launch, int64_t *bytes);
 int64_t mvf_kernel_launches(void);
 
+/* Autotuner record (no reference counterpart): the first K/M SpMM of each precision
+ * and batch width on a context times every kernel variant on the real operands and
+ * keeps the fastest; this returns "fp32 R=2: chunked 227.1 us, direct 173.9 us, ...
+ * pick vec/G=8; ..." -- every candidate's time per launch and the choice, for the
+ * tunings made so far (the string is owned by the context). */
+const char *mvf_spmm_tuning(mvf_ctx *ctx);
+
+/* Parity hook for the autotuner's candidates (no reference counterpart): y = A_f x
+ * for R right-hand sides (R a power of two <= 32) with SpMM variant `variant`
+ * (0 chunked, 1 direct [R <= 4], 2..5 G = 4/8/16/32 lanes per row [R <= 16]) in FP64
+ * (fp64 = 1: K, M and vectors FP64) or FP32 (K, M, vectors complex64); w is the
+ * frequency's omega, rounded to FP32 when the mesh's quirks carry MVF_Q_FP32_CONST,
+ * as in assembly.  x, y: host [nne][R] complex. */
+int mvf_spmm_variant(mvf_ctx *ctx, int32_t f, int32_t variant, int32_t fp64, int32_t R, const double *x,
+                     double *y);
+
 /* y = A_f x like mvf_spmv, for callers that cannot let the library allocate device
  * memory (a host whose device memory is owned by its own pool, or code between
  * captured / latency-critical stream steps).  No counterpart in the reference.

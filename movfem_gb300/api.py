@@ -53,7 +53,9 @@ class Stats(ctypes.Structure):
 
 EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numbering", "mvf_set_sigma",
            "mvf_assemble", "mvf_export_coo", "mvf_export_rhs", "mvf_element_matrices", "mvf_solve",
-           "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches", "mvf_spmv_noalloc"]
+           "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches", "mvf_spmv_noalloc",
+           "mvf_spmm_tuning", "mvf_spmm_variant"]
+SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
 
 
 def kernel_launches() -> int:
@@ -97,8 +99,11 @@ def load(build: bool = True):
     L.mvf_spmv_noalloc.argtypes = [P, I32, P, P]
     L.mvf_kernel_launches.argtypes = []
     L.mvf_kernel_launches.restype = I64
+    L.mvf_spmm_variant.argtypes = [P, I32, I32, I32, I32, P, P]
+    L.mvf_spmm_tuning.argtypes = [P]
+    L.mvf_spmm_tuning.restype = ctypes.c_char_p
     for n in EXPORTS:
-        if n not in ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches"):
+        if n not in ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning"):
             getattr(L, n).restype = ctypes.c_int
     _lib = L
     return L
@@ -224,6 +229,17 @@ class MTProblem:
         b = ctypes.c_int64()
         self._chk(self.L.mvf_profile_spmm(self.h, f, reps, ctypes.byref(s), ctypes.byref(b)))
         return {"seconds_per_launch": s.value, "bytes_per_launch": b.value}
+
+    def spmm_variant(self, f: int, variant: int, fp64: bool, x: np.ndarray) -> np.ndarray:
+        """y = A_f x with one SpMM candidate; x: [nne, R] complex, R a power of two."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.empty_like(x)
+        self._chk(self.L.mvf_spmm_variant(self.h, f, variant, int(fp64), x.shape[1], _p(x), _p(y)))
+        return y
+
+    def spmm_tuning(self) -> str:
+        """The SpMM variants the autotuner picked on this context so far."""
+        return self.L.mvf_spmm_tuning(self.h).decode()
 
     def impedance(self, rx=None, with_fields: bool = False):
         rx = self.mesh.rx if rx is None else np.asarray(rx, dtype=np.float64)

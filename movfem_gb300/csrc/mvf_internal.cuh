@@ -105,6 +105,10 @@ struct Ctx {
     int64_t npatch = 0, patch_entries = 0;
     int patch_max = 0;
     std::vector<int64_t> pcolor_off;
+    // SpMM variant chosen by timing, per [FP64?][log2 R]; -1 = not tuned yet
+    int spmm_pick[2][6] = {{-1, -1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1, -1}};
+    float spmm_us[2][6] = {};
+    std::string spmm_note;
 };
 
 // process-wide count of the library's kernel launches

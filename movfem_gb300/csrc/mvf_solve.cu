@@ -153,6 +153,111 @@ __global__ void __launch_bounds__(256) spmm_km_direct(int32_t n, const int64_t *
     }
 }
 
+// R consecutive complex values x[0..R) into registers with the widest aligned loads
+// (16-byte runs: two complex64 or one complex128 per load).
+template <class T, class TV, int R>
+__device__ __forceinline__ void load_run(const TV *__restrict__ p, TV (&v)[R]) {
+    if constexpr (sizeof(TV) == 8 && R % 2 == 0) {
+        const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+        for (int i = 0; i < R / 2; ++i) {
+            const float4 t = __ldg(q + i);
+            v[2 * i].x = t.x;
+            v[2 * i].y = t.y;
+            v[2 * i + 1].x = t.z;
+            v[2 * i + 1].y = t.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < R; ++i) v[i] = p[i];
+    }
+}
+
+// G lanes per row, 32/G rows per warp, every lane carrying all R right-hand sides:
+// each nonzero costs one column index, one K and one M value, and one contiguous
+// R-complex run of x -- against R copies of the index and values when lanes are split
+// over the right-hand sides.  The group's partial sums meet by xor-shuffles; lane j of
+// the group writes right-hand sides j, j+G, ...
+template <class T, class TV, int R, int G>
+__global__ void __launch_bounds__(256) spmm_km_vec(int32_t n, const int64_t *__restrict__ rowptr,
+                                                    const int32_t *__restrict__ col, const T *__restrict__ K,
+                                                    const T *__restrict__ M, const TV *__restrict__ x,
+                                                    const TV *__restrict__ b, TV *__restrict__ y, int use_w32) {
+    constexpr int RPW = 32 / G;
+    const int lane = threadIdx.x & 31, g = lane / G, j = lane % G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
+        const int64_t row = base + g;
+        int64_t k0 = 0, k1 = 0;
+        if (row < n) {
+            k0 = __ldg(rowptr + row);
+            k1 = __ldg(rowptr + row + 1);
+        }
+        T kr[R], ki[R], mr[R], mi[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) kr[r] = ki[r] = mr[r] = mi[r] = T(0);
+        int64_t k = k0 + j;
+        for (; k + G < k1; k += 2 * G) {
+            const int c0 = __ldg(col + k), c1 = __ldg(col + k + G);
+            const T kv0 = __ldg(K + k), mv0 = __ldg(M + k), kv1 = __ldg(K + k + G), mv1 = __ldg(M + k + G);
+            TV x0[R], x1[R];
+            load_run<T, TV, R>(x + (int64_t)c0 * R, x0);
+            load_run<T, TV, R>(x + (int64_t)c1 * R, x1);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                kr[r] += kv0 * x0[r].x + kv1 * x1[r].x;
+                ki[r] += kv0 * x0[r].y + kv1 * x1[r].y;
+                mr[r] += mv0 * x0[r].x + mv1 * x1[r].x;
+                mi[r] += mv0 * x0[r].y + mv1 * x1[r].y;
+            }
+        }
+        if (k < k1) {
+            const int c0 = __ldg(col + k);
+            const T kv0 = __ldg(K + k), mv0 = __ldg(M + k);
+            TV x0[R];
+            load_run<T, TV, R>(x + (int64_t)c0 * R, x0);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                kr[r] += kv0 * x0[r].x;
+                ki[r] += kv0 * x0[r].y;
+                mr[r] += mv0 * x0[r].x;
+                mi[r] += mv0 * x0[r].y;
+            }
+        }
+        // (K + i w M) x: fold w in before the reduction
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const T w = use_w32 ? (T)c_sp.w32[r] : (T)c_sp.omega[r];
+            kr[r] -= w * mi[r];
+            ki[r] += w * mr[r];
+        }
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1)
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                kr[r] += __shfl_xor_sync(0xffffffffu, kr[r], o);
+                ki[r] += __shfl_xor_sync(0xffffffffu, ki[r], o);
+            }
+        if (row < n) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (r % G != j) continue;
+                TV out;
+                if (b) {
+                    const TV bv = b[row * R + r];
+                    out.x = bv.x - kr[r];
+                    out.y = bv.y - ki[r];
+                } else {
+                    out.x = kr[r];
+                    out.y = ki[r];
+                }
+                y[row * R + r] = out;
+            }
+        }
+    }
+}
+
 // diagonal entries of K and M
 __global__ void extract_diag(int32_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
                              const double *__restrict__ K, const double *__restrict__ M, double *__restrict__ kd,
@@ -544,20 +649,105 @@ static int alloc_work(Ctx *c, Work &W, int R, int m) {
     return 0;
 }
 
+// SpMM variants: 0 chunked (spmm_km), 1 direct (R <= 4), 2..5 vec with G = 4, 8, 16,
+// 32 lanes per row (R <= 16).
+constexpr int SPMM_VARIANTS = 6;
+static const char *const spmm_names[SPMM_VARIANTS] = {"chunked", "direct", "vec/G=4", "vec/G=8", "vec/G=16",
+                                                      "vec/G=32"};
+
+static bool spmm_ok(int v, int R) { return v == 0 || (v == 1 && R <= 4) || (v >= 2 && R <= 16); }
+
+template <class T, class TV, int R>
+static void spmm_variant(Ctx *c, int v, const T *K, const T *M, const TV *x, const TV *b, TV *y, int use_w32) {
+    const int threads = 256;
+    const int G = v >= 2 ? (4 << (v - 2)) : 32;
+    const int64_t rows_per_block = (threads / 32) * (32 / G);
+    const unsigned grid = (unsigned)std::min<int64_t>((c->nne + rows_per_block - 1) / rows_per_block, 152 * 64);
+    count_launch();
+#define MVF_SPMM_ARGS <<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32)
+    switch (v) {
+        case 1:
+            if constexpr (R <= 4) spmm_km_direct<T, TV, R> MVF_SPMM_ARGS;
+            break;
+        case 2:
+            if constexpr (R <= 16) spmm_km_vec<T, TV, R, 4> MVF_SPMM_ARGS;
+            break;
+        case 3:
+            if constexpr (R <= 16) spmm_km_vec<T, TV, R, 8> MVF_SPMM_ARGS;
+            break;
+        case 4:
+            if constexpr (R <= 16) spmm_km_vec<T, TV, R, 16> MVF_SPMM_ARGS;
+            break;
+        case 5:
+            if constexpr (R <= 16) spmm_km_vec<T, TV, R, 32> MVF_SPMM_ARGS;
+            break;
+        default: spmm_km<T, TV, R> MVF_SPMM_ARGS; break;
+    }
+#undef MVF_SPMM_ARGS
+}
+
+template <class T, class TV>
+static void spmm_dispatch(Ctx *c, int v, int R, const T *K, const T *M, const TV *x, const TV *b, TV *y,
+                          int use_w32) {
+    switch (R) {
+        case 1: spmm_variant<T, TV, 1>(c, v, K, M, x, b, y, use_w32); break;
+        case 2: spmm_variant<T, TV, 2>(c, v, K, M, x, b, y, use_w32); break;
+        case 4: spmm_variant<T, TV, 4>(c, v, K, M, x, b, y, use_w32); break;
+        case 8: spmm_variant<T, TV, 8>(c, v, K, M, x, b, y, use_w32); break;
+        case 16: spmm_variant<T, TV, 16>(c, v, K, M, x, b, y, use_w32); break;
+        default: spmm_variant<T, TV, 32>(c, v, K, M, x, b, y, use_w32); break;
+    }
+}
+
+// y = A x or b - A x.  The first product of a given precision and batch width on a
+// context times every applicable variant on the real operands (one warm-up and three
+// timed launches each, CUDA events on the context's stream) and keeps the fastest;
+// y is simply rewritten by each trial (x and b are never aliased with y).  Inside a
+// stream capture nothing is timed: the untuned default runs and the choice stays open.
 template <class T, class TV>
 static void launch_spmm(Ctx *c, int R, const T *K, const T *M, const TV *x, const TV *b, TV *y, int use_w32) {
-    const int threads = 256;
-    const int64_t rows_per_block = threads / 32;
-    count_launch();
-    const unsigned grid = (unsigned)std::min<int64_t>((c->nne + rows_per_block - 1) / rows_per_block, 152 * 64);
-    switch (R) {
-        case 1: spmm_km_direct<T, TV, 1><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
-        case 2: spmm_km_direct<T, TV, 2><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
-        case 4: spmm_km_direct<T, TV, 4><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
-        case 8: spmm_km<T, TV, 8><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
-        case 16: spmm_km<T, TV, 16><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
-        default: spmm_km<T, TV, 32><<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32); break;
+    int li = 0;
+    while ((1 << li) < R && li < 5) ++li;
+    const int fp64 = sizeof(T) == 8;
+    int &pick = c->spmm_pick[fp64][li];
+    if (pick < 0) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(c->stream, &cs);
+        if (cs != cudaStreamCaptureStatusNone) {
+            spmm_dispatch<T, TV>(c, R <= 4 ? 1 : 0, R, K, M, x, b, y, use_w32);
+            return;
+        }
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        int best = R <= 4 ? 1 : 0;
+        float best_ms = 1e30f;
+        char line[96];
+        std::snprintf(line, sizeof line, "%s R=%d:", fp64 ? "fp64" : "fp32", R);
+        c->spmm_note += line;
+        if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+            for (int v = 0; v < SPMM_VARIANTS; ++v) {
+                if (!spmm_ok(v, R)) continue;
+                spmm_dispatch<T, TV>(c, v, R, K, M, x, b, y, use_w32);
+                cudaEventRecord(e0, c->stream);
+                for (int t = 0; t < 3; ++t) spmm_dispatch<T, TV>(c, v, R, K, M, x, b, y, use_w32);
+                cudaEventRecord(e1, c->stream);
+                float ms = 0;
+                if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) break;
+                std::snprintf(line, sizeof line, " %s %.1f us,", spmm_names[v], (double)ms * 1e3 / 3);
+                c->spmm_note += line;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = v;
+                }
+            }
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        pick = best;
+        c->spmm_us[fp64][li] = best_ms * 1e3f / 3;
+        std::snprintf(line, sizeof line, " pick %s; ", spmm_names[best]);
+        c->spmm_note += line;
     }
+    spmm_dispatch<T, TV>(c, pick, R, K, M, x, b, y, use_w32);
 }
 
 static unsigned grid_for(int64_t n) { return (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 32); }
@@ -837,6 +1027,57 @@ extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mod
 }
 
 extern "C" int64_t mvf_kernel_launches(void) { return launch_counter().load(); }
+
+extern "C" const char *mvf_spmm_tuning(mvf_ctx *xc) { return xc ? xc->c.spmm_note.c_str() : ""; }
+
+extern "C" int mvf_spmm_variant(mvf_ctx *xc, int32_t f, int32_t variant, int32_t fp64, int32_t R, const double *x,
+                                double *y) {
+    if (!xc || !x || !y) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
+    if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
+    if (R < 1 || R > MAXR || (R & (R - 1)) || variant < 0 || variant >= SPMM_VARIANTS || !spmm_ok(variant, R))
+        return fail(c, MVF_E_ARG, "bad variant / right-hand-side count");
+    const MatrixSet *S = nullptr;
+    for (const MatrixSet &s : c->sets)
+        if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
+    SolveParams sp{};
+    for (int r = 0; r < R; ++r) {
+        sp.omega[r] = c->omega[f];
+        sp.w32[r] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
+    }
+    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    const size_t nv = (size_t)c->nne * R;
+    if (fp64) {
+        double2 *dx, *dy;
+        MVF_CUDA(c, cudaMalloc((void **)&dx, nv * sizeof(double2)));
+        MVF_CUDA(c, cudaMalloc((void **)&dy, nv * sizeof(double2)));
+        MVF_CUDA(c, cudaMemcpyAsync(dx, x, nv * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+        spmm_dispatch<double, double2>(c, variant, R, S->K64, S->M64, dx, nullptr, dy, 1);
+        MVF_CUDA(c, cudaMemcpyAsync(y, dy, nv * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+        MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+        cudaFree(dx);
+        cudaFree(dy);
+    } else {
+        std::vector<float2> hx(nv), hy(nv);
+        for (size_t i = 0; i < nv; ++i) hx[i] = make_float2((float)x[2 * i], (float)x[2 * i + 1]);
+        float2 *dx, *dy;
+        MVF_CUDA(c, cudaMalloc((void **)&dx, nv * sizeof(float2)));
+        MVF_CUDA(c, cudaMalloc((void **)&dy, nv * sizeof(float2)));
+        MVF_CUDA(c, cudaMemcpyAsync(dx, hx.data(), nv * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+        spmm_dispatch<float, float2>(c, variant, R, S->K32, S->M32, dx, nullptr, dy, 1);
+        MVF_CUDA(c, cudaMemcpyAsync(hy.data(), dy, nv * sizeof(float2), cudaMemcpyDeviceToHost, c->stream));
+        MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+        cudaFree(dx);
+        cudaFree(dy);
+        for (size_t i = 0; i < nv; ++i) {
+            y[2 * i] = hy[i].x;
+            y[2 * i + 1] = hy[i].y;
+        }
+    }
+    MVF_CUDA(c, cudaGetLastError());
+    return 0;
+}
 
 extern "C" int mvf_profile_spmm(mvf_ctx *xc, int32_t f, int32_t reps, double *sec_per_launch, int64_t *bytes) {
     if (!xc || !sec_per_launch || reps < 1) return MVF_E_ARG;

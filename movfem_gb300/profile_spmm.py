@@ -34,7 +34,8 @@ def main():
     r = p.profile_spmm(0, reps=a.reps)
     print(json.dumps({"cells": a.cells, "nne": p.nne, "nnz": p.nnz, "rhs": 2 * a.freqs,
                       "us_per_launch": r["seconds_per_launch"] * 1e6, "bytes_per_launch": r["bytes_per_launch"],
-                      "GBps": r["bytes_per_launch"] / r["seconds_per_launch"] / 1e9}))
+                      "GBps": r["bytes_per_launch"] / r["seconds_per_launch"] / 1e9,
+                      "tuning": p.spmm_tuning()}))
 
 
 if __name__ == "__main__":

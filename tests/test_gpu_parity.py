@@ -116,6 +116,32 @@ def test_spmv_matches_cpu_product(mn):
     assert _rel(y, ref) < 1e-12
 
 
+@pytest.mark.parametrize("mn", [8, 20])
+def test_every_spmm_variant_matches_cpu_product(mn):
+    """Each autotuner candidate, FP64 and FP32, every batch width it accepts, against
+    the oracle's matrix: FP64 to 1e-12, FP32 (complex64 K, M and vectors) to 2e-6 of
+    |A||x| row-wise."""
+    m = models.box(mn, n=(3, 3, 2), seed=6)
+    w = 2 * math.pi * 0.5
+    p = _problem(m)
+    p.assemble([w])
+    A, _ = oracle.Oracle(m).matrix(w)
+    absA = abs(A)
+    rng = np.random.Generator(np.random.PCG64(8))
+    for R in (1, 2, 4, 8, 16, 32):
+        x = rng.normal(size=(p.nne, R)) + 1j * rng.normal(size=(p.nne, R))
+        ref = A @ x
+        scale = absA @ np.abs(x)
+        for v in api.SPMM_VARIANTS:
+            if (v == 1 and R > 4) or (v >= 2 and R > 16):
+                continue
+            y64 = p.spmm_variant(0, v, True, x)
+            assert _rel(y64, ref) < 1e-12, (R, api.SPMM_VARIANTS[v])
+            y32 = p.spmm_variant(0, v, False, x)
+            assert np.max(np.abs(y32 - ref) / scale) < 2e-6, (R, api.SPMM_VARIANTS[v])
+    assert p.spmm_tuning() == "" or "R=" in p.spmm_tuning()
+
+
 def _c1_small():
     return M.plain_linear_block(ncells=8, d=250.0, n_air=4, dz_air=500.0, nrx=3)
 
