@@ -169,6 +169,35 @@ int mvf_spmm_variant(mvf_ctx *ctx, int32_t f, int32_t variant, int32_t fp64, int
  * Returns after the result is in y. */
 int mvf_spmv_noalloc(mvf_ctx *ctx, int32_t f, const double *x_dev, double *y_dev);
 
+/* Initial guess for the following mvf_solve calls (no counterpart in the reference:
+ * MUMPS needs none).  x0: host [nfreq][2][nne] complex for the assembled frequencies,
+ * copied to the device; the refinement loop then starts from b - A x0 instead of b.
+ * x0 = NULL drops the guess.  A guess stored for another frequency count is ignored. */
+int mvf_set_guess(mvf_ctx *ctx, const double *x0);
+
+/* ---- Learned warm start (no counterpart in the reference) -------------------------
+ * A dilated 3-D convolutional operator on a cell grid: nconv 3x3x3 convolutions of
+ * `width` channels with ReLU (dilations[l] each), then a 1x1x1 convolution to `cout`
+ * channels.  BF16 weights and activations, FP32 accumulation; training keeps FP32
+ * master weights and runs Adam.  Grids are channels-last [X][Y][Z][c], FP32 on the
+ * host.  Parameters are laid out layer by layer: weights [3^3 or 1][cin][cout], then
+ * the bias [cout]. */
+typedef struct mvf_net mvf_net;
+int mvf_net_create(mvf_net **net, int32_t cin, int32_t width, int32_t cout, int32_t nconv, const int32_t *dilations,
+                   uint64_t seed, int32_t device);
+void mvf_net_destroy(mvf_net *net);
+const char *mvf_net_last_error(mvf_net *net);
+int64_t mvf_net_num_params(mvf_net *net);
+int mvf_net_get_params(mvf_net *net, float *params);
+int mvf_net_set_params(mvf_net *net, const float *params); /* also resets Adam */
+int mvf_net_forward(mvf_net *net, int32_t X, int32_t Y, int32_t Z, const float *in, float *out);
+/* loss = mean over all outputs of (out - target)^2, and d loss / d params (FP32) */
+int mvf_net_gradients(mvf_net *net, int32_t X, int32_t Y, int32_t Z, const float *in, const float *target,
+                      float *loss, float *grad);
+/* forward + backward + one Adam step (beta 0.9 / 0.999, eps 1e-8) at learning rate lr */
+int mvf_net_train_step(mvf_net *net, int32_t X, int32_t Y, int32_t Z, const float *in, const float *target, float lr,
+                       float *loss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,7 +54,11 @@ class Stats(ctypes.Structure):
 EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numbering", "mvf_set_sigma",
            "mvf_assemble", "mvf_export_coo", "mvf_export_rhs", "mvf_element_matrices", "mvf_solve",
            "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches", "mvf_spmv_noalloc",
-           "mvf_spmm_tuning", "mvf_spmm_variant"]
+           "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
+           "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
+           "mvf_net_gradients", "mvf_net_train_step"]
+_NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
+               "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params")
 SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
 
 
@@ -100,10 +104,23 @@ def load(build: bool = True):
     L.mvf_kernel_launches.argtypes = []
     L.mvf_kernel_launches.restype = I64
     L.mvf_spmm_variant.argtypes = [P, I32, I32, I32, I32, P, P]
+    L.mvf_set_guess.argtypes = [P, P]
+    L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
+    L.mvf_net_destroy.argtypes = [P]
+    L.mvf_net_destroy.restype = None
+    L.mvf_net_last_error.argtypes = [P]
+    L.mvf_net_last_error.restype = ctypes.c_char_p
+    L.mvf_net_num_params.argtypes = [P]
+    L.mvf_net_num_params.restype = I64
+    L.mvf_net_get_params.argtypes = [P, P]
+    L.mvf_net_set_params.argtypes = [P, P]
+    L.mvf_net_forward.argtypes = [P, I32, I32, I32, P, P]
+    L.mvf_net_gradients.argtypes = [P, I32, I32, I32, P, P, P, P]
+    L.mvf_net_train_step.argtypes = [P, I32, I32, I32, P, P, ctypes.c_float, P]
     L.mvf_spmm_tuning.argtypes = [P]
     L.mvf_spmm_tuning.restype = ctypes.c_char_p
     for n in EXPORTS:
-        if n not in ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning"):
+        if n not in _NOT_STATUS:
             getattr(L, n).restype = ctypes.c_int
     _lib = L
     return L
@@ -236,6 +253,16 @@ class MTProblem:
         y = np.empty_like(x)
         self._chk(self.L.mvf_spmm_variant(self.h, f, variant, int(fp64), x.shape[1], _p(x), _p(y)))
         return y
+
+    def set_guess(self, x0: np.ndarray | None):
+        """Initial guess [nfreq, 2, nne] complex for the following solves (None drops it)."""
+        if x0 is None:
+            self._chk(self.L.mvf_set_guess(self.h, None))
+            return
+        x0 = np.ascontiguousarray(x0, dtype=np.complex128)
+        if x0.shape != (self.omega.size, 2, self.nne):
+            raise ValueError(f"guess must be [{self.omega.size}, 2, {self.nne}]")
+        self._chk(self.L.mvf_set_guess(self.h, _p(x0)))
 
     def spmm_tuning(self) -> str:
         """The SpMM variants the autotuner picked on this context so far."""

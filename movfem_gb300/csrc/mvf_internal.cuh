@@ -71,6 +71,7 @@ struct Device {
     // right-hand sides and solutions: [nfreq][2][nne] complex
     double *rhs = nullptr;
     double *x = nullptr;
+    double *guess = nullptr;  // optional initial guess, same layout (mvf_set_guess)
     // element matrices of the last assembly, kept for the parity hook
     double *Ke = nullptr, *Me = nullptr, *be = nullptr;
     // vertex patches (Schwarz preconditioner of the 36/54-DOF elements)
@@ -94,6 +95,7 @@ struct Ctx {
     Device d;
     // assembly state
     int nfreq = 0;
+    int guess_nfreq = 0;  // frequencies the stored initial guess covers
     double omega[MVF_MAX_FREQ] = {0};
     int ifreq0 = 0;
     std::vector<MatrixSet> sets;

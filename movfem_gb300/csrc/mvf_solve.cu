@@ -914,6 +914,17 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
                                     (size_t)W.n * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
     }
     MVF_CUDA(c, cudaMemsetAsync(W.x64, 0, (size_t)W.n * R * sizeof(double2), c->stream));
+    if (c->d.guess && c->guess_nfreq == c->nfreq) {
+        // initial guess (e.g. the learned warm start): refinement starts from b - A x0
+        if (npol == 2) {
+            count_launch();
+            gather_rhs<<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>(W.n, R, Rreal, f0, (const double2 *)c->d.guess,
+                                                                         W.x64);
+        } else {
+            MVF_CUDA(c, cudaMemcpyAsync(W.x64, (const double2 *)c->d.guess + ((int64_t)f0 * 2 + pol0) * W.n,
+                                        (size_t)W.n * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
+        }
+    }
     std::vector<double> bn(R, 1.0), rel(R, 0.0), est(R, 0.0);
     {
         const int64_t vs = (int64_t)W.n * R;
@@ -1027,6 +1038,28 @@ extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mod
 }
 
 extern "C" int64_t mvf_kernel_launches(void) { return launch_counter().load(); }
+
+extern "C" int mvf_set_guess(mvf_ctx *xc, const double *x0) {
+    if (!xc) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (!x0) {
+        if (c->d.guess) cudaFree(c->d.guess);
+        c->d.guess = nullptr;
+        c->guess_nfreq = 0;
+        return 0;
+    }
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble before setting an initial guess");
+    const size_t vb = (size_t)c->nfreq * 2 * c->nne * sizeof(double2);
+    if (c->d.guess && c->guess_nfreq != c->nfreq) {
+        cudaFree(c->d.guess);
+        c->d.guess = nullptr;
+    }
+    if (!c->d.guess) MVF_CUDA(c, cudaMalloc((void **)&c->d.guess, vb));
+    MVF_CUDA(c, cudaMemcpyAsync(c->d.guess, x0, vb, cudaMemcpyHostToDevice, c->stream));
+    MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->guess_nfreq = c->nfreq;
+    return 0;
+}
 
 extern "C" const char *mvf_spmm_tuning(mvf_ctx *xc) { return xc ? xc->c.spmm_note.c_str() : ""; }
 
