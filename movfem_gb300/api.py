@@ -228,7 +228,9 @@ class MTProblem:
         rc = self.L.mvf_solve(self.h, _p(buf), tol, mode, max_iters, ctypes.byref(st))
         if not (rc == E_NOCONV and not raise_noconv):
             self._chk(rc)
-        return buf, st.as_dict()
+        d = st.as_dict()
+        d["converged"] = rc == 0
+        return buf, d
 
     def solve_device(self, tol: float = 1e-10, mode: int = MODE_MIXED, max_iters: int = 5000):
         """Solve with the assembled right-hand sides; the solutions stay on the device

@@ -364,14 +364,51 @@ __global__ void __launch_bounds__(256) multidot(int32_t n, int R, int k, const T
         double sr[JC], si[JC];
 #pragma unroll
         for (int q = 0; q < JC; ++q) sr[q] = si[q] = 0.0;
-        for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
-            const TV b = w[q];
+        if constexpr (sizeof(TV) == 8) {
+            // complex64 vectors: products and runs of up to 4 terms in FP32, every run
+            // added into the FP64 sums (FP64 arithmetic is scarce on GB300; the FP32
+            // products carry the same relative error as the complex64 entries)
+            float fr[JC], fi[JC];
+            int run = 0;
+#pragma unroll
+            for (int q = 0; q < JC; ++q) fr[q] = fi[q] = 0.f;
+            for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot;
+                 q += (int64_t)gridDim.x * blockDim.x) {
+                const TV b = w[q];
+#pragma unroll
+                for (int jj = 0; jj < JC; ++jj) {
+                    if (jj < jn) {
+                        const TV a = V[(int64_t)(j0 + jj) * vstride + q];
+                        fr[jj] = fmaf(a.x, b.x, fmaf(a.y, b.y, fr[jj]));
+                        fi[jj] = fmaf(a.x, b.y, fmaf(-a.y, b.x, fi[jj]));
+                    }
+                }
+                if (++run == 4) {
+#pragma unroll
+                    for (int jj = 0; jj < JC; ++jj) {
+                        sr[jj] += fr[jj];
+                        si[jj] += fi[jj];
+                        fr[jj] = fi[jj] = 0.f;
+                    }
+                    run = 0;
+                }
+            }
 #pragma unroll
             for (int jj = 0; jj < JC; ++jj) {
-                if (jj < jn) {
-                    const TV a = V[(int64_t)(j0 + jj) * vstride + q];
-                    sr[jj] += (double)a.x * b.x + (double)a.y * b.y;
-                    si[jj] += (double)a.x * b.y - (double)a.y * b.x;
+                sr[jj] += fr[jj];
+                si[jj] += fi[jj];
+            }
+        } else {
+            for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot;
+                 q += (int64_t)gridDim.x * blockDim.x) {
+                const TV b = w[q];
+#pragma unroll
+                for (int jj = 0; jj < JC; ++jj) {
+                    if (jj < jn) {
+                        const TV a = V[(int64_t)(j0 + jj) * vstride + q];
+                        sr[jj] += (double)a.x * b.x + (double)a.y * b.y;
+                        si[jj] += (double)a.x * b.y - (double)a.y * b.x;
+                    }
                 }
             }
         }
@@ -470,27 +507,33 @@ struct Hess {
     int active;
 };
 
+// The new column k runs through the k previous rotations, a chain of dependent
+// updates: it is held in shared memory (one column per right-hand side, lane r) so
+// the chain waits on shared-memory latency, and the rotations are read up front.
 __global__ void hessenberg_step(int R, int k, const double2 *__restrict__ hc, const double2 *__restrict__ wn2, Hess *hs) {
+    __shared__ double2 col[65][32];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R) return;
+    if (r >= R || threadIdx.x >= 32 || k > 63) return;
     Hess &S = hs[r];
-    for (int i = 0; i <= k; ++i) S.H[i][k] = hc[i * R + r];
-    S.H[k + 1][k] = make_double2(sqrt(fmax(wn2[r].x, 0.0)), 0.0);
+    const int l = threadIdx.x;
+    for (int i = 0; i <= k; ++i) col[i][l] = hc[i * R + r];
+    col[k + 1][l] = make_double2(sqrt(fmax(wn2[r].x, 0.0)), 0.0);
     // previous rotations: [c s; -conj(s) c] with c real
     for (int i = 0; i < k; ++i) {
         const double c = S.cs[i].x;
         const double2 s = S.sn[i];
-        const double2 a = S.H[i][k], b = S.H[i + 1][k];
+        const double2 a = col[i][l], b = col[i + 1][l];
         double2 t1, t2;
         t1.x = c * a.x + (s.x * b.x - s.y * b.y);
         t1.y = c * a.y + (s.x * b.y + s.y * b.x);
         t2.x = -(s.x * a.x + s.y * a.y) + c * b.x;
         t2.y = -(s.x * a.y - s.y * a.x) + c * b.y;
-        S.H[i][k] = t1;
-        S.H[i + 1][k] = t2;
+        col[i][l] = t1;
+        col[i + 1][l] = t2;
     }
-    const double2 a = S.H[k][k];
-    const double bb = S.H[k + 1][k].x;  // real and >= 0
+    for (int i = 0; i < k; ++i) S.H[i][k] = col[i][l];
+    const double2 a = col[k][l];
+    const double bb = col[k + 1][l].x;  // real and >= 0
     const double na = hypot(a.x, a.y);
     double c;
     double2 s;
@@ -609,9 +652,16 @@ struct Work {
     size_t vb = 0;
     double2 *pinvs = nullptr;  // vertex-patch inverses, one set per frequency
     int npol = 2, nfi = 1;
+    // captured blocks of Arnoldi steps (see fgmres_cycle)
+    static constexpr int GCH = 10, MAXB = 8;
+    cudaGraphExec_t blocks[MAXB] = {};
+    int64_t block_launches[MAXB] = {};
+    int cycles = 0;
 };
 
 static void free_work(Work &W) {
+    for (cudaGraphExec_t &g : W.blocks)
+        if (g) cudaGraphExecDestroy(g);
     void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs,
                  W.pinvs};
     for (void *q : p)
@@ -625,8 +675,10 @@ static int alloc_work(Ctx *c, Work &W, int R, int m) {
     W.R = R;
     W.m = m;
     W.n = c->nne;
-    // reduction blocks: about 16 vector entries per thread, at most 4 per SM
-    W.nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(152 * 4, ((int64_t)c->nne * R + 4095) / 4096));
+    // reduction blocks: at least 2 vector entries per thread, at most 4 blocks per SM.
+    // The projections are FP64 arithmetic, which GB300 runs at a small fraction of
+    // its FP32 rate, so small systems must still spread over every SM.
+    W.nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(152 * 4, ((int64_t)c->nne * R + 511) / 512));
     const size_t nv = (size_t)W.n * R;
     W.vb = nv * sizeof(TV);
     MVF_CUDA(c, cudaMalloc(&W.V, W.vb * (m + 1)));
@@ -820,9 +872,8 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
     count_launch();
     scale_into<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, w, W.nrm, V);
     std::vector<Hess> hh(R);
-    std::vector<double> beta(R);
-    int k = 0;
-    for (k = 0; k < m; ++k) {
+    // one Arnoldi step: z_k = P v_k, w = A z_k, orthogonalise, v_{k+1} = w / ||w||
+    auto step = [&](int k) -> int {
         precondition<TV>(c, W, V + k * vs, Z + k * vs);
         launch_spmm<T, TV>(c, R, K, M, Z + k * vs, (const TV *)nullptr, w, use_w32);
         int rc = cgs2<TV>(c, W, k + 1);
@@ -831,19 +882,54 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
         hessenberg_step<<<1, 32, 0, c->stream>>>(R, k, W.hc, W.nrm, W.hs);
         count_launch();
         scale_into<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, w, W.nrm, V + (k + 1) * vs);
-        // check the residual estimate every 10 iterations and at the end
-        if ((k + 1) % 10 == 0 || k + 1 == m) {
-            MVF_CUDA(c, cudaMemcpyAsync(hh.data(), W.hs, sizeof(Hess) * R, cudaMemcpyDeviceToHost, c->stream));
-            MVF_CUDA(c, cudaStreamSynchronize(c->stream));
-            bool all = true;
-            for (int r = 0; r < R; ++r) {
-                const double g = hypot(hh[r].g[k + 1].x, hh[r].g[k + 1].y);
-                est[r] = hh[r].beta > 0 ? g / hh[r].beta : 0.0;
-                if (est[r] > tol_abs_rel) all = false;
+        return 0;
+    };
+    int k = 0;
+    // blocks of GCH steps between residual checks; from the second cycle of a solve on
+    // (the SpMM is tuned by then and every pointer is fixed) each block is captured
+    // once as a CUDA graph and replayed, one launch instead of ~10 per step
+    while (k < m) {
+        const int k1 = std::min(k + Work::GCH, m), kb = k / Work::GCH;
+        bool done = false;
+        if (W.cycles > 0 && kb < Work::MAXB && k % Work::GCH == 0) {
+            if (!W.blocks[kb]) {
+                const int64_t c0 = launch_counter().load();
+                cudaGraph_t g = nullptr;
+                if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                    int rc = 0;
+                    for (int kk = k; kk < k1 && !rc; ++kk) rc = step(kk);
+                    const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+                    const int64_t nk = launch_counter().load() - c0;
+                    launch_counter().fetch_sub(nk);  // counted again at each replay
+                    if (e == cudaSuccess && !rc && g && cudaGraphInstantiate(&W.blocks[kb], g, 0) == cudaSuccess)
+                        W.block_launches[kb] = nk;
+                    else
+                        W.blocks[kb] = nullptr;
+                    if (g) cudaGraphDestroy(g);
+                    cudaGetLastError();
+                }
             }
-            if (all) { ++k; break; }
+            if (W.blocks[kb] && cudaGraphLaunch(W.blocks[kb], c->stream) == cudaSuccess) {
+                launch_counter().fetch_add(W.block_launches[kb]);
+                done = true;
+            }
         }
+        if (!done)
+            for (int kk = k; kk < k1; ++kk)
+                if (int rc = step(kk)) return rc;
+        k = k1;
+        // residual estimate after the block
+        MVF_CUDA(c, cudaMemcpyAsync(hh.data(), W.hs, sizeof(Hess) * R, cudaMemcpyDeviceToHost, c->stream));
+        MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+        bool all = true;
+        for (int r = 0; r < R; ++r) {
+            const double g = hypot(hh[r].g[k].x, hh[r].g[k].y);
+            est[r] = hh[r].beta > 0 ? g / hh[r].beta : 0.0;
+            if (est[r] > tol_abs_rel) all = false;
+        }
+        if (all) break;
     }
+    ++W.cycles;
     count_launch();
     hessenberg_solve<<<1, 32, 0, c->stream>>>(R, k, W.hs, W.y);
     count_launch();

@@ -240,16 +240,18 @@ def evaluate(net: WarmStartNet, seeds, tol: float = 1e-10, mode: int = api.MODE_
         p = api.MTProblem(m, device=0)
         p.assemble([2 * math.pi * f])
         rhs = np.stack([p.export_rhs(0)])[0]
-        st0 = p.solve_device(tol=tol, mode=mode, max_iters=5000)
+        x, st0 = p.solve(None, tol=tol, mode=mode, max_iters=5000, raise_noconv=False)
         gne = p.numbering()
         xhat = dof_field(gne, p.nne, net.forward(features(m, f)))
         x0 = fitted_guess(p, xhat, rhs)
         r0 = max(np.linalg.norm(rhs[k] - p.spmv(0, x0)[k]) / np.linalg.norm(rhs[k]) for k in range(2))
+        e0 = max(np.linalg.norm(x0[k] - x[0, k]) / np.linalg.norm(x[0, k]) for k in range(2))
         p.set_guess(x0[None])
         st1 = p.solve_device(tol=tol, mode=mode, max_iters=5000)
         rows.append({"seed": s, "iters_plain": st0["inner_iters"], "iters_learned": st1["inner_iters"],
                      "res_plain": st0["rel_residual"], "res_learned": st1["rel_residual"],
-                     "converged": bool(st0["converged"] and st1["converged"]), "initial_rel_residual": r0})
+                     "converged": bool(st0["converged"] and st1["converged"]), "initial_rel_residual": r0,
+                     "initial_rel_error": e0})
         p.close()
     return rows
 
@@ -262,12 +264,13 @@ def main():
     ap.add_argument("--test", type=int, default=16)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--width", type=int, default=32)
     ap.add_argument("--save", default="")
     a = ap.parse_args()
     t0 = time.time()
     data = [make_sample(1000 + i)[:2] for i in range(a.train)]
     t1 = time.time()
-    net = WarmStartNet()
+    net = WarmStartNet(width=a.width)
     hist = train(net, data, epochs=a.epochs, lr=a.lr)
     t2 = time.time()
     rows = evaluate(net, [900000 + i for i in range(a.test)])
@@ -277,6 +280,7 @@ def main():
                       "loss_last": hist[-1], "epochs": len(hist), "mean_iters_plain": ip, "mean_iters_learned": il,
                       "iteration_ratio": il / ip, "all_converged": all(r["converged"] for r in rows),
                       "mean_initial_rel_residual": float(np.mean([r["initial_rel_residual"] for r in rows])),
+                      "mean_initial_rel_error": float(np.mean([r["initial_rel_error"] for r in rows])),
                       "rows": rows}))
     if a.save:
         np.save(a.save, net.params())
