@@ -56,7 +56,8 @@ typedef struct mvf_mesh {
     const double *sigma;      /* [npt][6] complex: g_sigma(6,g_npt) */
     const double *mu;         /* [npt][6]: g_mu(6,g_npt) */
     int32_t dirichlet;        /* PARAM.INP boundary: 1 Dirichlet, 0 GPML */
-    int32_t inimod;           /* Dirichlet primary model; 1 (zero secondary field) is built */
+    int32_t inimod;           /* Dirichlet primary model: 1 zero secondary field, 2 half-space,
+                                 3 layered (bd_inimod, boundary_conds.f90:188-250,396-598) */
     int32_t gpml_sch;         /* 0 Fang, 1 Zhou */
     double a0, b0, nn;        /* GPML parameters */
     int32_t nextd;            /* extension cells per side */
@@ -64,6 +65,11 @@ typedef struct mvf_mesh {
     int32_t nzl_air;          /* g_nzl(g_nsf-1) */
     double ztop;              /* g_ztop */
     int32_t quirks;           /* MVF_Q_* */
+    /* Dirichlet primary models 2/3 (PARAM.INP; unused otherwise): */
+    double h_sigma;           /* inimod 2: half-space conductivity */
+    int32_t nlayers;          /* inimod 3: number of layers (1..16) */
+    const double *l_sigma;    /* inimod 3: [nlayers] layer conductivities, top first */
+    const double *l_dz;       /* inimod 3: [nlayers-1] layer thicknesses (m) */
 } mvf_mesh;
 
 typedef struct mvf_stats {

@@ -39,7 +39,8 @@ class _Mesh(ctypes.Structure):
         ("mu", ctypes.c_void_p), ("dirichlet", ctypes.c_int32), ("inimod", ctypes.c_int32),
         ("gpml_sch", ctypes.c_int32), ("a0", ctypes.c_double), ("b0", ctypes.c_double), ("nn", ctypes.c_double),
         ("nextd", ctypes.c_int32), ("nzl_top", ctypes.c_int32), ("nzl_air", ctypes.c_int32),
-        ("ztop", ctypes.c_double), ("quirks", ctypes.c_int32),
+        ("ztop", ctypes.c_double), ("quirks", ctypes.c_int32), ("h_sigma", ctypes.c_double),
+        ("nlayers", ctypes.c_int32), ("l_sigma", ctypes.c_void_p), ("l_dz", ctypes.c_void_p),
     ]
 
 
@@ -141,9 +142,11 @@ class MTProblem:
         zp = np.ascontiguousarray(mesh.zp, dtype=np.float64)
         sg = np.ascontiguousarray(mesh.sigma, dtype=np.complex128)
         mu = np.ascontiguousarray(mesh.mu, dtype=np.float64)
+        ls = None if mesh.l_sigma is None else np.ascontiguousarray(mesh.l_sigma, dtype=np.float64)
+        ld = None if mesh.l_dz is None else np.ascontiguousarray(mesh.l_dz, dtype=np.float64)
         m = _Mesh(mesh.nodes_per_elem, mesh.nx, mesh.ny, mesh.nz, _p(xp), _p(yp), _p(zp), _p(sg), _p(mu),
                   mesh.dirichlet, mesh.inimod, mesh.gpml_sch, mesh.a0, mesh.b0, mesh.nn, mesh.nextd, mesh.nzl_top,
-                  mesh.nzl_air, mesh.ztop, mesh.quirks)
+                  mesh.nzl_air, mesh.ztop, mesh.quirks, mesh.h_sigma, 0 if ls is None else ls.size, _p(ls), _p(ld))
         h = ctypes.c_void_p()
         rc = self.L.mvf_create(ctypes.byref(h), ctypes.byref(m), device)
         self.h = h

@@ -14,6 +14,7 @@
 // atomics, deterministic sums).
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 
@@ -43,6 +44,11 @@ struct AsmParams {
     int have_sigma_f;
     int64_t npt;
     GpmlParams g;
+    // Dirichlet primary models 2/3: prescribed boundary values lift into b
+    int lift, q9;
+    int64_t nb;
+    const int32_t *bidx;
+    const double2 *bep;
 };
 
 __constant__ AsmParams c_ap;
@@ -488,8 +494,33 @@ __global__ void __launch_bounds__(256) element_kernel(
             K64[lo] += Ks[t];
             M64[lo] += Ms[t];
         }
-        // right-hand side (assign_bi, global_assembly.f90:62-79); the Dirichlet lift is
-        // zero for the zero-secondary-field boundary and for GPML
+        // right-hand side (assign_bi, global_assembly.f90:62-79) minus the Dirichlet lift
+        // sum_jm A_e(j, jm) f_boundary(jm) (local_vfem, MoVFEM_3DMT.f90:221-263), which
+        // vanishes for the zero-secondary-field model and for GPML.  f_boundary
+        // (boundary_conds.f90:188-250) is the primary E_x (E_y) of the boundary node
+        // times dx/dxi_dir (dy/dxi_dir) of this element at that node; Jn holds the
+        // latter for every Dirichlet DOF not on a z face.
+        double *Jn = &S.srcw[0][0][0][0];  // [ME][2], free after the Gauss-point loop
+        if (c_ap.lift) {
+            for (int jm = tid; jm < ME; jm += blockDim.x) {
+                const int bd = -S.gne[jm];
+                double j0 = 0.0, j1 = 0.0;
+                if (bd > 0 && bd != 3 && bd != 6) {
+                    const int nd = edge_node[jm], dir = edge_dir[jm];
+                    const double rn[3] = {(double)node_ref(nd, 0), (double)node_ref(nd, 1), (double)node_ref(nd, 2)};
+                    for (int l = 0; l < MN; ++l) {
+                        double N, g[3];
+                        nodal(MN, l, rn, N, g, c_ap.q9 != 0);
+                        j0 += g[dir] * S.x[l][0];
+                        j1 += g[dir] * S.x[l][1];
+                    }
+                    if (c_ap.bidx[S.node[nd]] < 0) atomicMax(errflag, 5);
+                }
+                Jn[2 * jm] = j0;
+                Jn[2 * jm + 1] = j1;
+            }
+            __syncthreads();
+        }
 #pragma unroll
         for (int q = 0; q < BPT; ++q) {
             const int s = tid + q * 256;
@@ -498,9 +529,24 @@ __global__ void __launch_bounds__(256) element_kernel(
                 const int gj = S.gne[j];
                 if (gj > 0) {
                     for (int f = 0; f < nf; ++f) {
+                        double lr = 0.0, li = 0.0;
+                        if (c_ap.lift) {
+                            const double w = rr32(c_ap.omega[f]);
+                            for (int jm = 0; jm < ME; ++jm) {
+                                const double jn = Jn[2 * jm + p];
+                                if (jn == 0.0) continue;
+                                const int32_t bi = c_ap.bidx[S.node[edge_node[jm]]];
+                                if (bi < 0) continue;
+                                const double2 ep = c_ap.bep[((int64_t)f * c_ap.nb + bi) * 2 + p];
+                                // (K + i w M)(j, jm) * ep * jn
+                                const double ar = Ks[j * ME + jm], ai = w * Ms[j * ME + jm];
+                                lr += (ar * ep.x - ai * ep.y) * jn;
+                                li += (ar * ep.y + ai * ep.x) * jn;
+                            }
+                        }
                         double *dst = rhs + (((int64_t)f * 2 + p) * nne + (gj - 1)) * 2;
-                        dst[0] += bacc[q][f][0];
-                        dst[1] += bacc[q][f][1];
+                        dst[0] += bacc[q][f][0] - lr;
+                        dst[1] += bacc[q][f][1] - li;
                     }
                 }
             }
@@ -577,6 +623,11 @@ static void set_params(Ctx *c, AsmParams &ap, int fset, int nfb, const double *o
     ap.omega_km = omegas[0];
     ap.r32 = (m.quirks & MVF_Q_FP32_CONST) ? 1 : 0;
     ap.have_sigma_f = c->d.sigma_f ? 1 : 0;
+    ap.lift = dirichlet_lift(*c) ? 1 : 0;
+    ap.q9 = (m.quirks & MVF_Q_LIN_DZETA) ? 1 : 0;
+    ap.nb = (int64_t)c->bnode_h.size();
+    ap.bidx = c->d.bidx;
+    ap.bep = c->d.bep;
     (void)fset;
     GpmlParams &g = ap.g;
     g.on = gpml;
@@ -684,6 +735,7 @@ int assemble_set(Ctx *c, MatrixSet &S, bool gpml, int fset) {
     if (herr == 1) return fail(c, MVF_E_SINGULAR, "no mu inversion: singular mu tensor (problem.f90:266-271)");
     if (herr == 2) return fail(c, MVF_E_SINGULAR, "no transformation: zero Jacobian (n_fem.f90:374-377)");
     if (herr == 4) return fail(c, MVF_E_STATE, "element entry missing from the CSR pattern");
+    if (herr == 5) return fail(c, MVF_E_STATE, "Dirichlet DOF off the x/y boundary planes");
     return 0;
 }
 
@@ -733,6 +785,117 @@ int element_matrices(Ctx *c, int64_t e0, int64_t count, int f, double *K, double
 
 using namespace mvf;
 
+// ---------------------------------------------------------------------------
+// Primary field of the Dirichlet models 2 (half-space under air) and 3 (layered
+// earth) on the boundary, per frequency (bd_setmodel / bd_updatemodel,
+// boundary_conds.f90:396-430; wait_recursion :521-553; ezl :558-598; p_pfields
+// :436-516).  Heights are depths below ztop in km, as the reference evaluates them.
+namespace {
+using cplx = std::complex<double>;
+
+struct Primary {
+    int nl = 0;
+    cplx psig[16], cz[16], ez[16];
+    double zl[16] = {0}, dl[16] = {0};
+    double pmu = 4.0 * M_PI * 1.e-7;
+};
+
+double q32(const Ctx *c, double v) { return (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)v : v; }
+
+void primary_model(const Ctx *c, double omega, Primary &L) {
+    const double eps0 = 8.854187817e-12;
+    const cplx I(0.0, 1.0);
+    if (c->mesh.inimod == 2) {
+        L.nl = 2;
+        L.psig[0] = I * q32(c, eps0 * omega);
+        L.psig[1] = q32(c, c->mesh.h_sigma) + I * q32(c, eps0 * omega);
+        return;
+    }
+    L.nl = (int)c->l_sigma_h.size();
+    L.zl[0] = 0.0;
+    for (int i = 0; i + 1 < L.nl; ++i) L.dl[i] = c->l_dz_h[i];
+    for (int i = 1; i < L.nl; ++i) L.zl[i] = L.zl[i - 1] - L.dl[i - 1];
+    for (int i = 0; i < L.nl; ++i) L.psig[i] = q32(c, c->l_sigma_h[i]) + I * q32(c, eps0 * omega);
+    // impedance recursion from the bottom layer up, then the field ratios downwards
+    const int nl = L.nl;
+    L.cz[nl - 1] = 1.0 / std::sqrt(I * (omega * L.pmu * L.psig[nl - 1]));
+    for (int l = nl - 2; l >= 0; --l) {
+        const cplx gl = std::sqrt(I * (omega * L.pmu * L.psig[l]));
+        const cplx r = (1.0 - gl * L.cz[l + 1]) / (1.0 + gl * L.cz[l + 1]);
+        const cplx ex = std::exp(-2.0 * gl * L.dl[l]);
+        L.cz[l] = (1.0 - r * ex) / (gl * (1.0 + r * ex));
+    }
+    L.ez[0] = 1.0;
+    for (int l = 0; l + 1 < nl; ++l) {
+        const cplx gl = std::sqrt(I * (omega * L.pmu * L.psig[l]));
+        L.ez[l + 1] = std::exp(-gl * L.dl[l]) * (L.ez[l] * L.cz[l + 1] * (1.0 + L.cz[l] * gl)) /
+                      (L.cz[l] * (1.0 + L.cz[l + 1] * gl));
+    }
+}
+
+// the layered model's field at height z (ezl, its field branch)
+cplx layered_e(const Primary &L, double omega, double z) {
+    const cplx I(0.0, 1.0);
+    cplx r = 0.0;
+    const int nl = L.nl;
+    for (int l = 0; l + 1 < nl; ++l) {
+        if (z <= L.zl[l] && z > L.zl[l + 1]) {
+            const cplx g = std::sqrt(I * (omega * L.pmu * L.psig[l]));
+            const cplx rr = (1.0 - g * L.cz[l + 1]) / (1.0 + g * L.cz[l + 1]);
+            r = (L.ez[l] / 2.0) * (1.0 + 1.0 / (L.cz[l] * g)) * (1.0 - rr * std::exp(-2.0 * g * (z - L.zl[l + 1]))) *
+                std::exp(-g * (L.zl[l] - z));
+        }
+    }
+    if (z <= L.zl[nl - 1]) {
+        const cplx g = std::sqrt(I * (omega * L.pmu * L.psig[nl - 1]));
+        r = L.ez[nl - 1] * std::exp(-g * (L.zl[nl - 1] - z));
+    }
+    return r;
+}
+
+// (E_x of polarisation 1, E_y of polarisation 2) at a node of height znode
+void boundary_field(const Ctx *c, const Primary &L, double omega, double znode, cplx out[2]) {
+    const cplx I(0.0, 1.0);
+    const double bb0 = 1.e-9, z = (c->mesh.ztop - znode) / 1000.0;
+    if (c->mesh.inimod == 2) {
+        cplx fp;
+        if (znode > c->mesh.ztop) {
+            const cplx sa = std::sqrt(I * (omega * L.pmu * L.psig[0]));
+            fp = (1.0 / sa) * (1.0 - z * sa);
+        } else {
+            const cplx sa = std::sqrt(I * (omega * L.pmu * L.psig[1]));
+            fp = (1.0 / sa) * std::exp(-z * sa);
+        }
+        out[0] = (I * q32(c, -2.0 * omega * bb0)) * fp;
+        out[1] = (I * q32(c, 2.0 * omega * bb0)) * fp;
+    } else {
+        const cplx f = znode > c->mesh.ztop ? (L.cz[0] - z) : L.cz[0] * layered_e(L, omega, z);
+        out[0] = (I * q32(c, 2.0 * omega * bb0)) * f;
+        out[1] = (I * q32(c, -2.0 * omega * bb0)) * f;
+    }
+}
+
+int boundary_fields(Ctx *c) {
+    if (c->d.bep) cudaFree(c->d.bep);
+    c->d.bep = nullptr;
+    if (!dirichlet_lift(*c)) return 0;
+    const int64_t nb = (int64_t)c->bnode_h.size();
+    std::vector<double2> h((size_t)c->nfreq * nb * 2);
+    for (int f = 0; f < c->nfreq; ++f) {
+        Primary L;
+        primary_model(c, c->omega[f], L);
+        for (int64_t b = 0; b < nb; ++b) {
+            cplx ep[2];
+            boundary_field(c, L, c->omega[f], c->zp_h[c->bnode_h[b]], ep);
+            for (int p = 0; p < 2; ++p) h[((size_t)f * nb + b) * 2 + p] = make_double2(ep[p].real(), ep[p].imag());
+        }
+    }
+    MVF_CUDA(c, cudaMalloc((void **)&c->d.bep, h.size() * sizeof(double2)));
+    MVF_CUDA(c, cudaMemcpy(c->d.bep, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    return 0;
+}
+}  // namespace
+
 extern "C" int mvf_assemble(mvf_ctx *x, int32_t nfreq, const double *omega, const double *sigma_f, int32_t ifreq0) {
     if (!x) return MVF_E_ARG;
     Ctx *c = &x->c;
@@ -758,6 +921,7 @@ extern "C" int mvf_assemble(mvf_ctx *x, int32_t nfreq, const double *omega, cons
     MVF_CUDA(c, cudaMalloc((void **)&c->d.x, vb));
     MVF_CUDA(c, cudaMemsetAsync(c->d.rhs, 0, vb, c->stream));
     MVF_CUDA(c, cudaMemsetAsync(c->d.x, 0, vb, c->stream));
+    if (int rc = boundary_fields(c)) return rc;
     const bool gpml = !c->mesh.dirichlet;
     if (!gpml) {
         // K and M do not depend on the frequency without GPML (Im(sigma) is dropped,

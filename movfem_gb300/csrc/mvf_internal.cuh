@@ -77,6 +77,11 @@ struct Device {
     // vertex patches (Schwarz preconditioner of the 36/54-DOF elements)
     int64_t *patch_ptr = nullptr, *patch_ioff = nullptr;
     int32_t *patch_dof = nullptr;
+    // Dirichlet primary models 2/3: node -> boundary-node index (-1 elsewhere) and the
+    // primary field there, [nfreq][nb][2] complex (E_x of the first polarisation, E_y
+    // of the second)
+    int32_t *bidx = nullptr;
+    double2 *bep = nullptr;
 };
 
 struct Ctx {
@@ -91,6 +96,8 @@ struct Ctx {
     int32_t ngn = 0;  // gradient nodes
     std::vector<int32_t> gne_h;  // [ne][me]
     std::vector<double> xp_h, yp_h, zp_h;  // host copies of the coordinates
+    std::vector<double> l_sigma_h, l_dz_h;  // layered primary model (inimod 3)
+    std::vector<int64_t> bnode_h;           // nodes on the x/y boundary planes (inimod 2/3)
     std::vector<int64_t> color_off;  // 9 offsets into elem_color
     Device d;
     // assembly state
@@ -132,6 +139,10 @@ int element_matrices(Ctx *c, int64_t e0, int64_t count, int f, double *K, double
     } while (0)
 
 void build_tables(int mn, int quirks, OrderTables &T);
+
+// Dirichlet primary models 2/3 (mvf_assemble.cu): true when the boundary DOFs carry
+// a non-zero prescribed value that lifts into the right-hand side
+inline bool dirichlet_lift(const Ctx &c) { return c.mesh.dirichlet && c.mesh.inimod != 1; }
 
 // assembly (mvf_assemble.cu)
 int assemble_set(Ctx *c, MatrixSet &S, bool gpml, int fset);

@@ -22,6 +22,11 @@ struct PostParams {
     int r32;
     int q9;
     double omega[MVF_MAX_FREQ];
+    // Dirichlet primary models 2/3: boundary-node index and primary field (f_boundary)
+    int lift;
+    int64_t nb;
+    const int32_t *bidx;
+    const double2 *bep;
 };
 __constant__ PostParams c_pp;
 
@@ -90,12 +95,33 @@ __device__ void node_E(const double *xp, const double *yp, const double *zp, con
     const int64_t nne = c_pp.nne;
     for (int j = 0; j < c_pp.me; ++j) {
         const int32_t g = gne[e * c_pp.me + j];
-        if (g <= 0) continue;  // Dirichlet DOF: f_boundary is zero for the zero-secondary-field model
+        double2 fb[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+        if (g <= 0) {
+            // Dirichlet DOF: f_boundary (boundary_conds.f90:188-250), zero for the
+            // zero-secondary-field model and on the z faces
+            const int bd = -g;
+            if (!c_pp.lift || bd == 3 || bd == 6) continue;
+            const int nd = edge_node[j], dir = edge_dir[j];
+            const int32_t bi = c_pp.bidx[ids[nd]];
+            if (bi < 0) continue;
+            const double rn[3] = {(double)node_ref(nd, 0), (double)node_ref(nd, 1), (double)node_ref(nd, 2)};
+            double jr[2] = {0.0, 0.0};
+            for (int l = 0; l < c_pp.mn; ++l) {
+                double N, gg[3];
+                nodal(c_pp.mn, l, rn, N, gg, c_pp.q9 != 0);
+                jr[0] += gg[dir] * X[l][0];
+                jr[1] += gg[dir] * X[l][1];
+            }
+            for (int p = 0; p < 2; ++p) {
+                const double2 ep = c_pp.bep[((int64_t)f * c_pp.nb + bi) * 2 + p];
+                fb[p] = make_double2(ep.x * jr[p], ep.y * jr[p]);
+            }
+        }
         double L, gL[3];
         const int dir = edge_dir[j];
         edge_factor(c_pp.mn, edge_node[j], dir, r, L, gL);
         for (int p = 0; p < 2; ++p) {
-            const double2 v = x[((int64_t)f * 2 + p) * nne + (g - 1)];
+            const double2 v = g > 0 ? x[((int64_t)f * 2 + p) * nne + (g - 1)] : fb[p];
             for (int a = 0; a < 3; ++a) {
                 const double ve = L * Ji[a][dir];
                 E[p][a].x += v.x * ve;
@@ -290,6 +316,10 @@ extern "C" int mvf_impedance(mvf_ctx *xc, int32_t nrx, const double *xr, const d
     pp.nny = c->nny; pp.nnz_nodes = c->nnz_nodes; pp.nne = c->nne;
     pp.r32 = (m.quirks & MVF_Q_FP32_CONST) ? 1 : 0;
     pp.q9 = (m.quirks & MVF_Q_LIN_DZETA) ? 1 : 0;
+    pp.lift = dirichlet_lift(*c) && c->d.bep ? 1 : 0;
+    pp.nb = (int64_t)c->bnode_h.size();
+    pp.bidx = c->d.bidx;
+    pp.bep = c->d.bep;
     for (int f = 0; f < c->nfreq; ++f) pp.omega[f] = c->omega[f];
     MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_pp, &pp, sizeof pp, 0, cudaMemcpyHostToDevice, c->stream));
     int *d_re;

@@ -361,8 +361,10 @@ static int create(Ctx *c, const mvf_mesh *m, int device) {
     if (m->nodes_per_elem != 8 && m->nodes_per_elem != 20 && m->nodes_per_elem != 27)
         return fail(c, MVF_E_ARG, "nodes_per_elem must be 8, 20 or 27");
     if (m->nx < 1 || m->ny < 1 || m->nz < 1) return fail(c, MVF_E_ARG, "empty mesh");
-    if (m->dirichlet && m->inimod != 1)
-        return fail(c, MVF_E_UNSUPPORTED, "Dirichlet primary models 2/3 are not built (inimod must be 1)");
+    if (m->dirichlet && (m->inimod < 1 || m->inimod > 3)) return fail(c, MVF_E_ARG, "inimod must be 1, 2 or 3");
+    if (m->dirichlet && m->inimod == 3 &&
+        (m->nlayers < 1 || m->nlayers > 16 || !m->l_sigma || (m->nlayers > 1 && !m->l_dz)))
+        return fail(c, MVF_E_ARG, "inimod 3 needs 1..16 layers with l_sigma[nlayers] and l_dz[nlayers-1]");
     if (!m->dirichlet && (m->nzl_top < 0 || m->nextd < 0)) return fail(c, MVF_E_ARG, "bad GPML zone sizes");
     c->mesh = *m;
     {
@@ -378,6 +380,12 @@ static int create(Ctx *c, const mvf_mesh *m, int device) {
         c->mesh.zp = c->zp_h.data();
         c->mesh.sigma = nullptr;
         c->mesh.mu = nullptr;
+        if (m->dirichlet && m->inimod == 3) {
+            c->l_sigma_h.assign(m->l_sigma, m->l_sigma + m->nlayers);
+            if (m->nlayers > 1) c->l_dz_h.assign(m->l_dz, m->l_dz + m->nlayers - 1);
+        }
+        c->mesh.l_sigma = nullptr;
+        c->mesh.l_dz = nullptr;
     }
     int ndev = 0;
     MVF_CUDA(c, cudaGetDeviceCount(&ndev));
@@ -423,6 +431,22 @@ static int create(Ctx *c, const mvf_mesh *m, int device) {
     if ((rc = upload(c, &c->d.rowptr, rowptr.data(), rowptr.size()))) return rc;
     if ((rc = upload(c, &c->d.col, col.data(), col.size()))) return rc;
     if ((rc = upload(c, &c->d.gne, c->gne_h.data(), c->gne_h.size()))) return rc;
+    if (dirichlet_lift(*c)) {
+        // nodes on the x and y boundary planes carry the prescribed primary field of
+        // the Dirichlet DOFs on faces 1, 2, 4, 5 (f_boundary skips the z faces 3, 6)
+        std::vector<int32_t> bidx(c->npt, -1);
+        c->bnode_h.clear();
+        for (int64_t i = 0; i < c->nnx; ++i)
+            for (int64_t j = 0; j < c->nny; ++j) {
+                if (i != 0 && i != c->nnx - 1 && j != 0 && j != c->nny - 1) continue;
+                for (int64_t k = 0; k < c->nnz_nodes; ++k) {
+                    const int64_t id = (i * c->nny + j) * c->nnz_nodes + k;
+                    bidx[id] = (int32_t)c->bnode_h.size();
+                    c->bnode_h.push_back(id);
+                }
+            }
+        if ((rc = upload(c, &c->d.bidx, bidx.data(), bidx.size()))) return rc;
+    }
     // element colouring: 2x2x2 parity classes share no DOF or node
     std::vector<int32_t> byc;
     byc.reserve(c->ne);
@@ -468,7 +492,7 @@ static void release(Ctx *c) {
     void *ptrs[] = {c->d.xp, c->d.yp, c->d.zp, c->d.sigma, c->d.sigma_f, c->d.mu, c->d.gne, c->d.elem_color,
                     c->d.N, c->d.dN, c->d.L, c->d.dL, c->d.gp, c->d.Gloc, c->d.edge_node, c->d.edge_dir,
                     c->d.rowptr, c->d.col, c->d.grow, c->d.gcol, c->d.gval, c->d.gtrow, c->d.gtcol, c->d.gtval,
-                    c->d.node_gidx, c->d.rhs, c->d.x, c->d.guess, c->d.Ke, c->d.Me, c->d.be, c->d.patch_ptr,
+                    c->d.node_gidx, c->d.rhs, c->d.x, c->d.guess, c->d.bidx, c->d.bep, c->d.Ke, c->d.Me, c->d.be, c->d.patch_ptr,
                     c->d.patch_ioff, c->d.patch_dof};
     for (void *p : ptrs)
         if (p) cudaFree(p);

@@ -32,3 +32,20 @@ def test_header_compiles_as_c():
         src = os.path.join(d, "t.c")
         open(src, "w").write('#include "movfem_gpu.h"\nint main(void){mvf_mesh m; (void)m; return 0;}\n')
         subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-I", HDR, "-c", src, "-o", os.path.join(d, "t.o")])
+
+
+def test_mesh_struct_layout_matches_the_header():
+    """The ctypes mirror of mvf_mesh has the C struct's size and field offsets."""
+    import subprocess
+    import tempfile
+    fields = [f for f, _ in api._Mesh._fields_]
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.c")
+        body = "".join(f'printf("%zu\\n", offsetof(mvf_mesh, {f}));' for f in fields)
+        open(src, "w").write('#include <stddef.h>\n#include <stdio.h>\n#include "movfem_gpu.h"\n'
+                             'int main(void){printf("%zu\\n", sizeof(mvf_mesh));' + body + 'return 0;}\n')
+        exe = os.path.join(d, "t")
+        subprocess.check_call(["gcc", "-std=c99", "-I", HDR, src, "-o", exe])
+        out = [int(v) for v in subprocess.check_output([exe]).split()]
+    assert out[0] == ctypes.sizeof(api._Mesh)
+    assert out[1:] == [getattr(api._Mesh, f).offset for f in fields]

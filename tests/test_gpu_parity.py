@@ -215,3 +215,37 @@ def test_errors_are_reported():
     with pytest.raises(api.MVFError) as e:
         p.solve()
     assert e.value.code == api.E_STATE or isinstance(e.value, api.MVFError)
+
+
+def _primary_model(m, inimod):
+    m.inimod = inimod
+    if inimod == 2:
+        m.h_sigma = 0.02
+    else:
+        m.l_sigma = np.array([0.05, 0.5, 0.01])
+        m.l_dz = np.array([90.0, 150.0])
+    return m
+
+
+@pytest.mark.parametrize("mn", [8, 20])
+@pytest.mark.parametrize("inimod", [2, 3])
+def test_dirichlet_primary_models_assembly_and_receivers(mn, inimod):
+    """Dirichlet half-space (2) and layered (3) boundary values: the lift of the
+    prescribed boundary DOFs into b (local_vfem) and their use in the receivers'
+    nodal E (get_er), against the oracle."""
+    m = _primary_model(models.box(mn, n=(3, 3, 2), seed=9), inimod)
+    w = 2 * math.pi * np.array([0.5, 3.0])
+    p = _problem(m)
+    p.assemble(w)
+    o = oracle.Oracle(m)
+    for f in range(2):
+        _, rrhs = o.assemble(w[f], ifreq=f)
+        assert np.abs(rrhs).max() > 0
+        assert _rel(p.export_rhs(f), rrhs) < 1e-10
+    x, _ = p.solve(tol=1e-10, raise_noconv=False)
+    Z, rho, phi, E, H = p.impedance(with_fields=True)
+    for f in range(2):
+        Er, Hr, Zr, _, _ = o.receivers(w[f], x[f])
+        assert _rel(E[f], Er) < 1e-11
+        assert _rel(H[f], Hr) < 1e-11
+        assert _rel(Z[f], Zr) < 1e-11
