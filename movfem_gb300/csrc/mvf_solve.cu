@@ -511,7 +511,10 @@ struct Hess {
 // updates: it is held in shared memory (one column per right-hand side, lane r) so
 // the chain waits on shared-memory latency, and the rotations are read up front.
 __global__ void hessenberg_step(int R, int k, const double2 *__restrict__ hc, const double2 *__restrict__ wn2, Hess *hs) {
+    constexpr int RC = 16;  // rotations staged per chunk (static shared memory < 48 KB)
     __shared__ double2 col[65][32];
+    __shared__ double2 sn_s[RC][32];
+    __shared__ double cs_s[RC][32];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= R || threadIdx.x >= 32 || k > 63) return;
     Hess &S = hs[r];
@@ -520,8 +523,17 @@ __global__ void hessenberg_step(int R, int k, const double2 *__restrict__ hc, co
     col[k + 1][l] = make_double2(sqrt(fmax(wn2[r].x, 0.0)), 0.0);
     // previous rotations: [c s; -conj(s) c] with c real
     for (int i = 0; i < k; ++i) {
-        const double c = S.cs[i].x;
-        const double2 s = S.sn[i];
+        if (i % RC == 0) {
+            // stage the next RC rotations (independent loads, all in flight at once)
+#pragma unroll
+            for (int q = 0; q < RC; ++q)
+                if (i + q < k) {
+                    cs_s[q][l] = S.cs[i + q].x;
+                    sn_s[q][l] = S.sn[i + q];
+                }
+        }
+        const double c = cs_s[i % RC][l];
+        const double2 s = sn_s[i % RC][l];
         const double2 a = col[i][l], b = col[i + 1][l];
         double2 t1, t2;
         t1.x = c * a.x + (s.x * b.x - s.y * b.y);
@@ -565,24 +577,36 @@ __global__ void hessenberg_init(int R, const double2 *__restrict__ rn2, Hess *hs
     for (int i = 1; i < 65; ++i) hs[r].g[i] = make_double2(0.0, 0.0);
 }
 
-// back substitution: y = H(0:k,0:k)^-1 g(0:k), stored in yout[j][r]
+// back substitution: y = H(0:k,0:k)^-1 g(0:k), stored in yout[j][r].  One warp per
+// right-hand side (block r): for each row the lanes form the products with the known
+// y_j (j = lane, lane + 32) and a shuffle sum, so the row chain waits on one
+// reduction instead of k dependent loads.
 __global__ void hessenberg_solve(int R, int k, Hess *hs, double2 *__restrict__ yout) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R) return;
+    __shared__ double2 y[64];
+    const int r = blockIdx.x, lane = threadIdx.x;
+    if (r >= R || k > 64) return;
     Hess &S = hs[r];
-    double2 y[64];
     for (int i = k - 1; i >= 0; --i) {
-        double2 t = S.g[i];
-        for (int j = i + 1; j < k; ++j) {
-            const double2 h = S.H[i][j];
-            t.x -= h.x * y[j].x - h.y * y[j].y;
-            t.y -= h.x * y[j].y + h.y * y[j].x;
+        double tr = 0.0, ti = 0.0;
+        for (int j = i + 1 + lane; j < k; j += 32) {
+            const double2 h = S.H[i][j], v = y[j];
+            tr += h.x * v.x - h.y * v.y;
+            ti += h.x * v.y + h.y * v.x;
         }
-        const double2 d = S.H[i][i];
-        const double dd = d.x * d.x + d.y * d.y;
-        y[i] = dd > 0 ? make_double2((t.x * d.x + t.y * d.y) / dd, (t.y * d.x - t.x * d.y) / dd) : make_double2(0, 0);
+        for (int o = 16; o > 0; o >>= 1) {
+            tr += __shfl_xor_sync(0xffffffffu, tr, o);
+            ti += __shfl_xor_sync(0xffffffffu, ti, o);
+        }
+        if (lane == 0) {
+            const double2 g = S.g[i], d = S.H[i][i];
+            const double t_r = g.x - tr, t_i = g.y - ti;
+            const double dd = d.x * d.x + d.y * d.y;
+            y[i] = dd > 0 ? make_double2((t_r * d.x + t_i * d.y) / dd, (t_i * d.x - t_r * d.y) / dd)
+                          : make_double2(0, 0);
+        }
+        __syncwarp();
     }
-    for (int i = 0; i < k; ++i) yout[i * R + r] = y[i];
+    for (int i = lane; i < k; i += 32) yout[i * R + r] = y[i];
 }
 
 // x += sum_j y[j][r] Z_j   (x in FP64; Z in the Krylov precision)
@@ -931,7 +955,7 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
     }
     ++W.cycles;
     count_launch();
-    hessenberg_solve<<<1, 32, 0, c->stream>>>(R, k, W.hs, W.y);
+    hessenberg_solve<<<R, 32, 0, c->stream>>>(R, k, W.hs, W.y);
     count_launch();
     update_x<TV, double2><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, k, Z, vs, W.y, x, R, 0);
     MVF_CUDA(c, cudaGetLastError());
