@@ -139,6 +139,13 @@ int mvf_solve(mvf_ctx *ctx, double *rhs_inout, double tol, int32_t mode, int32_t
 int mvf_impedance(mvf_ctx *ctx, int32_t nrx, const double *xr, const double *yr, double *Z, double *rho,
                   double *phi, double *E, double *H);
 
+/* Full-volume fields (node_solution + z_rho_phi, solution.f90:18-69) on the last
+ * solution: E, H [nfreq][npt][2][3] complex at every node (first visiting element),
+ * Z [nfreq][npt][4] complex, rho / phi [nfreq][npt][4] from each node's horizontal
+ * fields.  Any output may be NULL.  write_solution's SOLUTION.OUT layout is produced
+ * from these by movfem_gb300.output. */
+int mvf_node_fields(mvf_ctx *ctx, double *E, double *H, double *Z, double *rho, double *phi);
+
 /* Parity hook: y = A_f x for frequency f in FP64 (x, y: [2][nne] complex, host). */
 int mvf_spmv(mvf_ctx *ctx, int32_t f, const double *x, double *y);
 

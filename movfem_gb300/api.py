@@ -57,7 +57,7 @@ EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numb
            "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches", "mvf_spmv_noalloc",
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
-           "mvf_net_gradients", "mvf_net_train_step"]
+           "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
                "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params")
 SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
@@ -106,6 +106,7 @@ def load(build: bool = True):
     L.mvf_kernel_launches.restype = I64
     L.mvf_spmm_variant.argtypes = [P, I32, I32, I32, I32, P, P]
     L.mvf_set_guess.argtypes = [P, P]
+    L.mvf_node_fields.argtypes = [P, P, P, P, P, P]
     L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
     L.mvf_net_destroy.argtypes = [P]
     L.mvf_net_destroy.restype = None
@@ -258,6 +259,18 @@ class MTProblem:
         y = np.empty_like(x)
         self._chk(self.L.mvf_spmm_variant(self.h, f, variant, int(fp64), x.shape[1], _p(x), _p(y)))
         return y
+
+    def node_fields(self):
+        """E, H [nfreq, npt, 2, 3], Z [nfreq, npt, 4], rho, phi [nfreq, npt, 4] at every
+        node of the mesh (node_solution + z_rho_phi)."""
+        nf, npt = self.omega.size, self.mesh.npt
+        E = np.empty((nf, npt, 2, 3), dtype=np.complex128)
+        H = np.empty((nf, npt, 2, 3), dtype=np.complex128)
+        Z = np.empty((nf, npt, 4), dtype=np.complex128)
+        rho = np.empty((nf, npt, 4))
+        phi = np.empty((nf, npt, 4))
+        self._chk(self.L.mvf_node_fields(self.h, _p(E), _p(H), _p(Z), _p(rho), _p(phi)))
+        return E, H, Z, rho, phi
 
     def set_guess(self, x0: np.ndarray | None):
         """Initial guess [nfreq, 2, nne] complex for the following solves (None drops it)."""

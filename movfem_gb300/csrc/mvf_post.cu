@@ -282,9 +282,189 @@ __global__ void receivers_kernel(const double *__restrict__ xp, const double *__
     }
 }
 
+static int set_post_params(Ctx *c) {
+    const mvf_mesh &m = c->mesh;
+    PostParams pp{};
+    pp.mn = c->T.mn; pp.me = c->T.me; pp.nord = c->T.nord;
+    pp.nx = m.nx; pp.ny = m.ny; pp.nz = m.nz;
+    pp.nny = c->nny; pp.nnz_nodes = c->nnz_nodes; pp.nne = c->nne;
+    pp.r32 = (m.quirks & MVF_Q_FP32_CONST) ? 1 : 0;
+    pp.q9 = (m.quirks & MVF_Q_LIN_DZETA) ? 1 : 0;
+    pp.lift = dirichlet_lift(*c) && c->d.bep ? 1 : 0;
+    pp.nb = (int64_t)c->bnode_h.size();
+    pp.bidx = c->d.bidx;
+    pp.bep = c->d.bep;
+    for (int f = 0; f < c->nfreq; ++f) pp.omega[f] = c->omega[f];
+    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_pp, &pp, sizeof pp, 0, cudaMemcpyHostToDevice, c->stream));
+    return 0;
+}
+
+// ---------------------------------------------------------------- full volume
+// node_solution + z_rho_phi (solution.f90:18-69): E at every node from its first
+// visiting element, then H from that element's nodal gradients applied to the nodes'
+// E (get_hr), and Z, rho, phi from the node's own horizontal fields (hor_fields,
+// solution.f90:440-455).  Two launches: E for all nodes, then H and Z.
+
+// Z (z[4]), rho, phi from e = (Ex1, Ex2, Ey1, Ey2), h likewise (get_impedance,
+// inv_matrix, get_res_phase: solution.f90:456-505)
+__device__ void impedance4(const double2 e[4], const double2 h[4], double omega, double2 z[4], double rho[4],
+                           double phi[4]) {
+    auto mul = [](double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+    auto dv = [](double2 a, double2 b) {
+        const double s = b.x * b.x + b.y * b.y;
+        return make_double2((a.x * b.x + a.y * b.y) / s, (a.y * b.x - a.x * b.y) / s);
+    };
+    auto add = [](double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); };
+    const double2 det = make_double2(mul(h[0], h[3]).x - mul(h[1], h[2]).x, mul(h[0], h[3]).y - mul(h[1], h[2]).y);
+    const double2 ih[4] = {dv(h[3], det), dv(make_double2(-h[1].x, -h[1].y), det),
+                           dv(make_double2(-h[2].x, -h[2].y), det), dv(h[0], det)};
+    z[0] = add(mul(ih[0], e[0]), mul(ih[2], e[1]));
+    z[1] = add(mul(ih[1], e[0]), mul(ih[3], e[1]));
+    z[2] = add(mul(ih[0], e[2]), mul(ih[2], e[3]));
+    z[3] = add(mul(ih[1], e[2]), mul(ih[3], e[3]));
+    const double pi = 3.1415926535897932384626433, mu0 = 4 * pi * 1.e-7;
+    for (int i = 0; i < 4; ++i) {
+        double rr = (1.0 / (omega * mu0)) * (z[i].x * z[i].x + z[i].y * z[i].y);
+        double ph = 0.0;
+        if (rr < 1.e-2) rr = 0.0;
+        else ph = atan(z[i].y / z[i].x) * (180.0 / pi);
+        rho[i] = rr;
+        phi[i] = ph;
+    }
+}
+
+__global__ void node_e_all(const double *__restrict__ xp, const double *__restrict__ yp,
+                           const double *__restrict__ zp, const int32_t *__restrict__ gne,
+                           const int32_t *__restrict__ edge_node, const int32_t *__restrict__ edge_dir,
+                           const double2 *__restrict__ x, int nf, int64_t npt, double2 *__restrict__ Eall) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nf * npt; q += (int64_t)gridDim.x * blockDim.x) {
+        const int f = (int)(q / npt);
+        const int64_t id = q % npt;
+        const int64_t I = id / (c_pp.nny * c_pp.nnz_nodes), J = (id / c_pp.nnz_nodes) % c_pp.nny,
+                      K = id % c_pp.nnz_nodes;
+        double2 E[2][3];
+        node_E(xp, yp, zp, gne, edge_node, edge_dir, x, f, I, J, K, E);
+        for (int p = 0; p < 2; ++p)
+            for (int a = 0; a < 3; ++a) Eall[(q * 2 + p) * 3 + a] = E[p][a];
+    }
+}
+
+__global__ void node_h_all(const double *__restrict__ xp, const double *__restrict__ yp,
+                           const double *__restrict__ zp, const double *__restrict__ mu, int nf, int64_t npt,
+                           const double2 *__restrict__ Eall, double2 *__restrict__ Hall, double2 *__restrict__ Zo,
+                           double *__restrict__ rho, double *__restrict__ phi) {
+    const int nord = c_pp.nord, mn = c_pp.mn;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nf * npt; q += (int64_t)gridDim.x * blockDim.x) {
+        const int f = (int)(q / npt);
+        const int64_t id = q % npt;
+        const int64_t I = id / (c_pp.nny * c_pp.nnz_nodes), J = (id / c_pp.nnz_nodes) % c_pp.nny,
+                      K = id % c_pp.nnz_nodes;
+        const int fi = first_elem(I, c_pp.nx), fj = first_elem(J, c_pp.ny), fk = first_elem(K, c_pp.nz);
+        double X[MVF_MAX_NODES][3];
+        int64_t ids[MVF_MAX_NODES];
+        elem_coords(xp, yp, zp, fi, fj, fk, X, ids);
+        const double r[3] = {-1.0 + 2.0 * (double)(I - (int64_t)fi * (nord - 1)) / (nord - 1),
+                             -1.0 + 2.0 * (double)(J - (int64_t)fj * (nord - 1)) / (nord - 1),
+                             -1.0 + 2.0 * (double)(K - (int64_t)fk * (nord - 1)) / (nord - 1)};
+        double Ji[3][3];
+        jac_inv(X, r, Ji);
+        double2 ef[2][3];
+        for (int p = 0; p < 2; ++p)
+            for (int a = 0; a < 3; ++a) ef[p][a] = make_double2(0.0, 0.0);
+        double mf1[6] = {0, 0, 0, 0, 0, 0};
+        for (int l = 0; l < mn; ++l) {
+            double N, g[3], dn[3];
+            nodal(mn, l, r, N, g, c_pp.q9 != 0);
+            for (int a = 0; a < 3; ++a) dn[a] = Ji[a][0] * g[0] + Ji[a][1] * g[1] + Ji[a][2] * g[2];
+            const double2 *El = Eall + ((int64_t)f * npt + ids[l]) * 6;
+            for (int p = 0; p < 2; ++p) {
+                const double2 *e3 = El + p * 3;
+                ef[p][0].x += e3[2].x * dn[1] - e3[1].x * dn[2];
+                ef[p][0].y += e3[2].y * dn[1] - e3[1].y * dn[2];
+                ef[p][1].x += e3[0].x * dn[2] - e3[2].x * dn[0];
+                ef[p][1].y += e3[0].y * dn[2] - e3[2].y * dn[0];
+                ef[p][2].x += e3[1].x * dn[0] - e3[0].x * dn[1];
+                ef[p][2].y += e3[1].y * dn[0] - e3[0].y * dn[1];
+            }
+            const double *m = mu + ids[l] * 6;
+            const double det = m[0] * (m[3] * m[5] - m[4] * m[4]) + m[1] * (m[2] * m[4] - m[1] * m[5]) +
+                               m[2] * (m[1] * m[4] - m[3] * m[2]);
+            const double inv[6] = {(m[3] * m[5] - m[4] * m[4]) / det, (m[2] * m[4] - m[1] * m[5]) / det,
+                                   (m[1] * m[4] - m[2] * m[3]) / det, (m[0] * m[5] - m[2] * m[2]) / det,
+                                   (m[2] * m[1] - m[0] * m[4]) / det, (m[3] * m[0] - m[1] * m[1]) / det};
+            for (int a = 0; a < 6; ++a) mf1[a] += N * inv[a];
+        }
+        const double fac = p32(-1.0 / c_pp.omega[f]);
+        const int P[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+        double2 H[2][3];
+        for (int p = 0; p < 2; ++p)
+            for (int a = 0; a < 3; ++a) {
+                double sr = 0, si = 0;
+                for (int b = 0; b < 3; ++b) {
+                    sr += -fac * mf1[P[a][b]] * ef[p][b].y;
+                    si += fac * mf1[P[a][b]] * ef[p][b].x;
+                }
+                H[p][a] = make_double2(sr, si);
+            }
+        if (Hall)
+            for (int p = 0; p < 2; ++p)
+                for (int a = 0; a < 3; ++a) Hall[(q * 2 + p) * 3 + a] = H[p][a];
+        const double2 *Eo = Eall + q * 6;
+        const double2 e[4] = {Eo[0], Eo[3], Eo[1], Eo[4]};
+        const double2 h[4] = {H[0][0], H[1][0], H[0][1], H[1][1]};
+        double2 z[4];
+        double rr[4], pp[4];
+        impedance4(e, h, c_pp.omega[f], z, rr, pp);
+        for (int i = 0; i < 4; ++i) {
+            if (Zo) Zo[q * 4 + i] = z[i];
+            if (rho) rho[q * 4 + i] = rr[i];
+            if (phi) phi[q * 4 + i] = pp[i];
+        }
+    }
+}
+
 }  // namespace mvf
 
 using namespace mvf;
+
+extern "C" int mvf_node_fields(mvf_ctx *xc, double *E, double *H, double *Z, double *rho, double *phi) {
+    if (!xc) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (!c->solved) return fail(c, MVF_E_STATE, "solve before evaluating node fields");
+    if (int rc = set_post_params(c)) return rc;
+    const int nf = c->nfreq;
+    const int64_t npt = c->npt, n = (int64_t)nf * npt;
+    double2 *dE = nullptr, *dH = nullptr, *dZ = nullptr;
+    double *drho = nullptr, *dphi = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(dE); cudaFree(dH); cudaFree(dZ); cudaFree(drho); cudaFree(dphi);
+    };
+    cudaError_t e = cudaMalloc((void **)&dE, n * 6 * sizeof(double2));
+    if (e == cudaSuccess && H) e = cudaMalloc((void **)&dH, n * 6 * sizeof(double2));
+    if (e == cudaSuccess && Z) e = cudaMalloc((void **)&dZ, n * 4 * sizeof(double2));
+    if (e == cudaSuccess && rho) e = cudaMalloc((void **)&drho, n * 4 * sizeof(double));
+    if (e == cudaSuccess && phi) e = cudaMalloc((void **)&dphi, n * 4 * sizeof(double));
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(c, e, "node field buffers");
+    }
+    const unsigned grid = (unsigned)std::min<int64_t>((n + 127) / 128, 152 * 32);
+    count_launch();
+    node_e_all<<<grid, 128, 0, c->stream>>>(c->d.xp, c->d.yp, c->d.zp, c->d.gne, c->d.edge_node, c->d.edge_dir,
+                                            (const double2 *)c->d.x, nf, npt, dE);
+    count_launch();
+    node_h_all<<<grid, 128, 0, c->stream>>>(c->d.xp, c->d.yp, c->d.zp, c->d.mu, nf, npt, dE, dH, dZ, drho, dphi);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && E) e = cudaMemcpyAsync(E, dE, n * 6 * sizeof(double2), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && H) e = cudaMemcpyAsync(H, dH, n * 6 * sizeof(double2), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && Z) e = cudaMemcpyAsync(Z, dZ, n * 4 * sizeof(double2), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && rho) e = cudaMemcpyAsync(rho, drho, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && phi) e = cudaMemcpyAsync(phi, dphi, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(c, e, "node fields");
+    return 0;
+}
 
 extern "C" int mvf_impedance(mvf_ctx *xc, int32_t nrx, const double *xr, const double *yr, double *Z, double *rho,
                              double *phi, double *E, double *H) {
@@ -310,18 +490,7 @@ extern "C" int mvf_impedance(mvf_ctx *xc, int32_t nrx, const double *xr, const d
         rxy[r * 6 + 2] = c->xp_h[ie * (nord - 1)]; rxy[r * 6 + 3] = c->xp_h[ie * (nord - 1) + nord - 1];
         rxy[r * 6 + 4] = c->yp_h[je * (nord - 1)]; rxy[r * 6 + 5] = c->yp_h[je * (nord - 1) + nord - 1];
     }
-    PostParams pp{};
-    pp.mn = c->T.mn; pp.me = c->T.me; pp.nord = nord;
-    pp.nx = m.nx; pp.ny = m.ny; pp.nz = m.nz;
-    pp.nny = c->nny; pp.nnz_nodes = c->nnz_nodes; pp.nne = c->nne;
-    pp.r32 = (m.quirks & MVF_Q_FP32_CONST) ? 1 : 0;
-    pp.q9 = (m.quirks & MVF_Q_LIN_DZETA) ? 1 : 0;
-    pp.lift = dirichlet_lift(*c) && c->d.bep ? 1 : 0;
-    pp.nb = (int64_t)c->bnode_h.size();
-    pp.bidx = c->d.bidx;
-    pp.bep = c->d.bep;
-    for (int f = 0; f < c->nfreq; ++f) pp.omega[f] = c->omega[f];
-    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_pp, &pp, sizeof pp, 0, cudaMemcpyHostToDevice, c->stream));
+    if (int rc = set_post_params(c)) return rc;
     int *d_re;
     double *d_rxy, *d_rho, *d_phi;
     double2 *d_Z, *d_E = nullptr, *d_H = nullptr;

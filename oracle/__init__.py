@@ -71,6 +71,8 @@ def lib():
             L.orc_assemble.argtypes = [P, P, P, I64, I32, D, I32, P, P]
             L.orc_receivers.restype = ctypes.c_int
             L.orc_receivers.argtypes = [P, P, I32, D, P, I32, P, P, P, P, P, P, P]
+            L.orc_node_fields.restype = ctypes.c_int
+            L.orc_node_fields.argtypes = [P, P, I32, D, P, P, P, P, P, P]
             L.orc_check_sharing.restype = D
             L.orc_check_sharing.argtypes = [P]
             _lib = L
@@ -203,6 +205,22 @@ class Oracle:
                                  _ptr(E), _ptr(H), _ptr(Z), _ptr(rho), _ptr(phi))
         if rc != 0:
             raise RuntimeError(f"oracle receivers failed rc={rc}")
+        return E, H, Z, rho, phi
+
+    def node_fields(self, omega, x):
+        """E, H [npt, 2, 3], Z [npt, 4], rho [npt, 4], phi [npt, 4] at every node."""
+        gne, nne = self.numbering()
+        npt = self.mesh.npt
+        xs = np.ascontiguousarray(np.asarray(x, dtype=np.complex128).reshape(-1))
+        E = np.empty((npt, 2, 3), dtype=np.complex128)
+        H = np.empty((npt, 2, 3), dtype=np.complex128)
+        Z = np.empty((npt, 4), dtype=np.complex128)
+        rho = np.empty((npt, 4))
+        phi = np.empty((npt, 4))
+        rc = lib().orc_node_fields(self._s(), _ptr(gne), nne, float(omega), _ptr(xs), _ptr(E), _ptr(H), _ptr(Z),
+                                   _ptr(rho), _ptr(phi))
+        if rc != 0:
+            raise RuntimeError(f"oracle node fields failed rc={rc}")
         return E, H, Z, rho, phi
 
     def check_sharing(self):

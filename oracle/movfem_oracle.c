@@ -1150,6 +1150,45 @@ int orc_receivers(const orc_mesh *m, const int32_t *gne, int32_t nne, double ome
     return 0;
 }
 
+/* node_solution + z_rho_phi (solution.f90:18-69): E and H at every node (first
+ * visiting element), then Z, rho, phi from the node's own horizontal fields
+ * (hor_fields, solution.f90:440-455).  E, H: [npt][2][3] complex; Z [npt][4] complex;
+ * rho, phi [npt][4].  Any output may be NULL. */
+int orc_node_fields(const orc_mesh *m, const int32_t *gne, int32_t nne, double omega, const double *xs, double *Eo,
+                    double *Ho, double *Zo, double *rho, double *phi) {
+    elem_tab t;
+    layered_ctx L;
+    int64_t nnx, nny, nnz, id;
+    const cplx *x = (const cplx *)xs;
+    if (get_tab(m->nodes_per_elem, &t)) return -1;
+    node_dims(m, t.nord, &nnx, &nny, &nnz);
+    primary_model(m, omega, &L);
+    for (id = 0; id < nnx * nny * nnz; id++) {
+        int64_t IX = id / (nny * nnz), JY = (id / nnz) % nny, Kk = id % nnz;
+        cplx E[2][3], H[2][3], z[4];
+        double rr[4], pp[4];
+        int pol, c, i;
+        node_E(m, &t, gne, nne, omega, &L, x, IX, JY, Kk, E);
+        if (node_H(m, &t, gne, nne, omega, &L, x, IX, JY, Kk, H)) return -2;
+        {
+            cplx ev[4] = {E[0][0], E[1][0], E[0][1], E[1][1]};
+            cplx hv[4] = {H[0][0], H[1][0], H[0][1], H[1][1]};
+            impedance(omega, ev, hv, z, rr, pp);
+        }
+        for (pol = 0; pol < 2; pol++)
+            for (c = 0; c < 3; c++) {
+                if (Eo) { Eo[((id * 2 + pol) * 3 + c) * 2] = creal(E[pol][c]); Eo[((id * 2 + pol) * 3 + c) * 2 + 1] = cimag(E[pol][c]); }
+                if (Ho) { Ho[((id * 2 + pol) * 3 + c) * 2] = creal(H[pol][c]); Ho[((id * 2 + pol) * 3 + c) * 2 + 1] = cimag(H[pol][c]); }
+            }
+        for (i = 0; i < 4; i++) {
+            if (Zo) { Zo[(id * 4 + i) * 2] = creal(z[i]); Zo[(id * 4 + i) * 2 + 1] = cimag(z[i]); }
+            if (rho) rho[id * 4 + i] = rr[i];
+            if (phi) phi[id * 4 + i] = pp[i];
+        }
+    }
+    return 0;
+}
+
 /* vf_check_sharing (v_fem.f90:556-863): basis vectors of the DOFs shared across each
  * - face, evaluated at the DOF's own node in both elements. */
 double orc_check_sharing(const orc_mesh *m) {

@@ -94,6 +94,11 @@ int orc_receivers(const orc_mesh *m, const int32_t *gne, int32_t nne, double ome
                   const double *x, int32_t nrx, const double *xr, const double *yr,
                   double *E, double *H, double *Z, double *rho, double *phi);
 
+/* node_solution + z_rho_phi (solution.f90:18-69): E, H [npt][2][3] complex, Z [npt][4]
+ * complex, rho, phi [npt][4] at every node; outputs may be NULL. */
+int orc_node_fields(const orc_mesh *m, const int32_t *gne, int32_t nne, double omega, const double *x,
+                    double *E, double *H, double *Z, double *rho, double *phi);
+
 /* Basis self-check of the reference's vf_check_sharing kind: maximum mismatch of the
  * tangential component of shared edge basis functions between face neighbours. */
 double orc_check_sharing(const orc_mesh *m);

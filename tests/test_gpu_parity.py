@@ -249,3 +249,26 @@ def test_dirichlet_primary_models_assembly_and_receivers(mn, inimod):
         assert _rel(E[f], Er) < 1e-11
         assert _rel(H[f], Hr) < 1e-11
         assert _rel(Z[f], Zr) < 1e-11
+
+
+@pytest.mark.parametrize("mn", [8, 20])
+@pytest.mark.parametrize("inimod", [1, 3])
+def test_full_volume_node_fields(mn, inimod):
+    """E, H, Z, rho, phi at every node (node_solution + z_rho_phi) from the GPU solution,
+    against the oracle on the same solution vector."""
+    m = models.box(mn, n=(3, 3, 2), seed=10)
+    if inimod != 1:
+        _primary_model(m, inimod)
+    w = 2 * math.pi * np.array([0.5, 3.0])
+    p = _problem(m)
+    p.assemble(w)
+    x, _ = p.solve(tol=1e-10, raise_noconv=False)
+    E, H, Z, rho, phi = p.node_fields()
+    o = oracle.Oracle(m)
+    for f in range(2):
+        Er, Hr, Zr, rr, pr = o.node_fields(w[f], x[f])
+        assert _rel(E[f], Er) < 1e-11
+        assert _rel(H[f], Hr) < 1e-11
+        assert _rel(Z[f], Zr) < 1e-9
+        np.testing.assert_allclose(rho[f], rr, rtol=1e-9, atol=0)
+        np.testing.assert_allclose(phi[f], pr, rtol=1e-9, atol=1e-9)

@@ -1,0 +1,43 @@
+"""SOLUTION.OUT writer (write_solution layout): edit descriptors and record shapes."""
+from __future__ import annotations
+
+import numpy as np
+
+from movfem_gb300 import output
+
+
+def test_edit_descriptors():
+    assert output.es(1.0) == "         1.00000E+00"
+    assert output.es(-2.5e-7) == "        -2.50000E-07"
+    assert output.es(0.0) == "         0.00000E+00"
+    assert output.es(6.02214076e123) == "         6.02214+123"
+    assert output.fw(12.345678) == "            12.34568"
+    assert output.fw(-0.5) == "            -0.50000"
+    assert len(output.es(1.0)) == 20 and len(output.fw(1.0)) == 20
+
+
+def test_block_layout_and_round_trip():
+    rng = np.random.Generator(np.random.PCG64(3))
+    npt = 5
+    E = rng.normal(size=(npt, 2, 3)) + 1j * rng.normal(size=(npt, 2, 3))
+    H = rng.normal(size=(npt, 2, 3)) + 1j * rng.normal(size=(npt, 2, 3))
+    Z = rng.normal(size=(npt, 4)) + 1j * rng.normal(size=(npt, 4))
+    rho = rng.uniform(0, 100, size=(npt, 4))
+    phi = rng.uniform(-90, 90, size=(npt, 4))
+    lines = output.solution_block(2, E, H, Z, rho, phi).splitlines()
+    assert lines[0] == " vector-fem solution:            2"
+    assert len(lines) == 1 + (1 + npt) * 3
+    assert len(lines[1]) == 24 * 15 and lines[1].startswith("     Re[Ex_(1)]")
+    rec = lines[2]
+    assert len(rec) == 24 * 20
+    vals = [float(rec[20 * i:20 * i + 20]) for i in range(24)]
+    ref = []
+    for p in range(2):
+        ref += [v for a in range(3) for v in (E[0, p, a].real, E[0, p, a].imag)]
+        ref += [v for a in range(3) for v in (H[0, p, a].real, H[0, p, a].imag)]
+    np.testing.assert_allclose(vals, ref, rtol=1e-5, atol=1e-5)
+    zrec = lines[2 + npt + 1]
+    assert len(zrec) == 8 * 20
+    rrec = lines[-1]
+    np.testing.assert_allclose([float(rrec[20 * i:20 * i + 20]) for i in range(8)],
+                               list(rho[-1]) + list(phi[-1]), atol=1e-5)
