@@ -132,6 +132,15 @@ int mvf_element_matrices(const mvf_ctx *ctx, int64_t e0, int64_t count, int32_t 
  * right-hand side at a time.  tol: FP64 relative residual target. */
 int mvf_solve(mvf_ctx *ctx, double *rhs_inout, double tol, int32_t mode, int32_t max_iters, mvf_stats *st);
 
+/* Solve n independent contexts (models of any size) concurrently: nthreads host
+ * threads take contexts from a queue, largest first, and run mvf_solve (with the
+ * assembled right-hand sides, solutions kept on the device) on each context's stream.
+ * No counterpart in the reference, which solves one model per run.  st: [n] or NULL.
+ * Returns the first error other than MVF_E_NOCONV, else MVF_E_NOCONV if any context
+ * stopped above tolerance, else 0.  Each context's error text stays in that context. */
+int mvf_solve_many(mvf_ctx **ctx, int32_t n, double tol, int32_t mode, int32_t max_iters, mvf_stats *st,
+                   int32_t nthreads);
+
 /* FP64 receiver evaluation (get_er / get_hr / interpolate_rx / get_impedance /
  * get_res_phase: solution.f90:207-505, receiver_data.f90:111-253) on the last
  * solution: Z [nfreq][nrx][4] complex, rho/phi [nfreq][nrx][4]; E, H optional

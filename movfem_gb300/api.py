@@ -57,7 +57,7 @@ EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numb
            "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches", "mvf_spmv_noalloc",
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
-           "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields"]
+           "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
                "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params")
 SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
@@ -107,6 +107,7 @@ def load(build: bool = True):
     L.mvf_spmm_variant.argtypes = [P, I32, I32, I32, I32, P, P]
     L.mvf_set_guess.argtypes = [P, P]
     L.mvf_node_fields.argtypes = [P, P, P, P, P, P]
+    L.mvf_solve_many.argtypes = [P, I32, D, I32, I32, P, I32]
     L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
     L.mvf_net_destroy.argtypes = [P]
     L.mvf_net_destroy.restype = None
@@ -130,6 +131,25 @@ def load(build: bool = True):
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+def solve_many(problems, tol: float = 1e-10, mode: int = 0, max_iters: int = 5000, nthreads: int = 8):
+    """Solve the assembled systems of several :class:`MTProblem` concurrently
+    (``mvf_solve_many``); solutions stay on the device.  Returns per-problem
+    statistics with a ``converged`` flag."""
+    L = load()
+    n = len(problems)
+    hs = (ctypes.c_void_p * n)(*[p.h for p in problems])
+    st = (Stats * n)()
+    rc = L.mvf_solve_many(hs, n, tol, mode, max_iters, st, nthreads)
+    if rc not in (0, E_NOCONV):
+        raise MVFError(rc, " / ".join(L.mvf_last_error(p.h).decode() for p in problems))
+    out = []
+    for i, p in enumerate(problems):
+        d = st[i].as_dict()
+        d["converged"] = d["rel_residual"] <= tol or bool(d["stagnated"])
+        out.append(d)
+    return out
 
 
 class MTProblem:

@@ -82,6 +82,8 @@ struct Device {
     // of the second)
     int32_t *bidx = nullptr;
     double2 *bep = nullptr;
+    // the solver's per-batch frequencies (SolveParams, mvf_solve.cu)
+    double *wsp = nullptr;
 };
 
 struct Ctx {

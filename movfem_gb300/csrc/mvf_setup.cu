@@ -400,6 +400,7 @@ static int create(Ctx *c, const mvf_mesh *m, int device) {
         if (stack < 4096) MVF_CUDA(c, cudaDeviceSetLimit(cudaLimitStackSize, 4096));
     }
     MVF_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    MVF_CUDA(c, cudaMalloc((void **)&c->d.wsp, 2 * 32 * sizeof(double)));
     build_tables(m->nodes_per_elem, m->quirks, c->T);
     const int nord = c->T.nord;
     c->nnx = (int64_t)m->nx * (nord - 1) + 1;
@@ -492,7 +493,7 @@ static void release(Ctx *c) {
     void *ptrs[] = {c->d.xp, c->d.yp, c->d.zp, c->d.sigma, c->d.sigma_f, c->d.mu, c->d.gne, c->d.elem_color,
                     c->d.N, c->d.dN, c->d.L, c->d.dL, c->d.gp, c->d.Gloc, c->d.edge_node, c->d.edge_dir,
                     c->d.rowptr, c->d.col, c->d.grow, c->d.gcol, c->d.gval, c->d.gtrow, c->d.gtcol, c->d.gtval,
-                    c->d.node_gidx, c->d.rhs, c->d.x, c->d.guess, c->d.bidx, c->d.bep, c->d.Ke, c->d.Me, c->d.be, c->d.patch_ptr,
+                    c->d.node_gidx, c->d.rhs, c->d.x, c->d.guess, c->d.bidx, c->d.bep, c->d.wsp, c->d.Ke, c->d.Me, c->d.be, c->d.patch_ptr,
                     c->d.patch_ioff, c->d.patch_dof};
     for (void *p : ptrs)
         if (p) cudaFree(p);

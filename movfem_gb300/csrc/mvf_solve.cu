@@ -10,6 +10,8 @@
 // Mode 0 runs the Krylov method in complex FP32 with FP64 reductions and an FP64
 // Hessenberg least-squares problem inside FP64 iterative refinement (true residual
 // b - A x in FP64).  Mode 1 is the plain FP64 method, one right-hand side at a time.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -31,11 +33,12 @@ struct C2<double> {
 
 constexpr int MAXR = 32;  // right-hand sides per batch
 
+// angular frequency of every right-hand side of a batch, exact and FP32-rounded; one
+// copy per context in device memory (solves on different contexts may overlap)
 struct SolveParams {
     double omega[MAXR];
     double w32[MAXR];
 };
-__constant__ SolveParams c_sp;
 
 // y = A x (b == nullptr) or y = b - A x for R right-hand sides sharing K, M.
 // One warp per row.  The warp loads 32 consecutive nonzeros (K, M, column) with
@@ -46,11 +49,12 @@ template <class T, class TV, int R>
 __global__ void __launch_bounds__(256) spmm_km(int32_t n, const int64_t *__restrict__ rowptr,
                                                 const int32_t *__restrict__ col, const T *__restrict__ K,
                                                 const T *__restrict__ M, const TV *__restrict__ x,
-                                                const TV *__restrict__ b, TV *__restrict__ y, int use_w32) {
+                                                const TV *__restrict__ b, TV *__restrict__ y, int use_w32,
+                                                const SolveParams *__restrict__ sp) {
     constexpr int SL = 32 / R;
     const int lane = threadIdx.x & 31;
     const int r = lane % R, s = lane / R;
-    const T w = use_w32 ? (T)c_sp.w32[r] : (T)c_sp.omega[r];
+    const T w = use_w32 ? (T)sp->w32[r] : (T)sp->omega[r];
     for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n;
          row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
         const int64_t k0 = rowptr[row], k1 = rowptr[row + 1];
@@ -105,11 +109,12 @@ template <class T, class TV, int R>
 __global__ void __launch_bounds__(256) spmm_km_direct(int32_t n, const int64_t *__restrict__ rowptr,
                                                        const int32_t *__restrict__ col, const T *__restrict__ K,
                                                        const T *__restrict__ M, const TV *__restrict__ x,
-                                                       const TV *__restrict__ b, TV *__restrict__ y, int use_w32) {
+                                                       const TV *__restrict__ b, TV *__restrict__ y, int use_w32,
+                                                const SolveParams *__restrict__ sp) {
     constexpr int SL = 32 / R;
     const int lane = threadIdx.x & 31;
     const int r = lane % R, s = lane / R;
-    const T w = use_w32 ? (T)c_sp.w32[r] : (T)c_sp.omega[r];
+    const T w = use_w32 ? (T)sp->w32[r] : (T)sp->omega[r];
     for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n;
          row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
         const int64_t k0 = rowptr[row], k1 = rowptr[row + 1];
@@ -182,7 +187,8 @@ template <class T, class TV, int R, int G>
 __global__ void __launch_bounds__(256) spmm_km_vec(int32_t n, const int64_t *__restrict__ rowptr,
                                                     const int32_t *__restrict__ col, const T *__restrict__ K,
                                                     const T *__restrict__ M, const TV *__restrict__ x,
-                                                    const TV *__restrict__ b, TV *__restrict__ y, int use_w32) {
+                                                    const TV *__restrict__ b, TV *__restrict__ y, int use_w32,
+                                                const SolveParams *__restrict__ sp) {
     constexpr int RPW = 32 / G;
     const int lane = threadIdx.x & 31, g = lane / G, j = lane % G;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -228,7 +234,7 @@ __global__ void __launch_bounds__(256) spmm_km_vec(int32_t n, const int64_t *__r
         // (K + i w M) x: fold w in before the reduction
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const T w = use_w32 ? (T)c_sp.w32[r] : (T)c_sp.omega[r];
+            const T w = use_w32 ? (T)sp->w32[r] : (T)sp->omega[r];
             kr[r] -= w * mi[r];
             ki[r] += w * mr[r];
         }
@@ -275,12 +281,13 @@ __global__ void extract_diag(int32_t n, const int64_t *__restrict__ rowptr, cons
 __global__ void build_inverse_diag(int32_t n, int32_t ngn, int R, const double *__restrict__ kd,
                                    const double *__restrict__ md, const double *__restrict__ kphi,
                                    const double *__restrict__ mphi, const double *__restrict__ mabs,
-                                   double2 *__restrict__ dinv, double2 *__restrict__ pinv) {
+                                   double2 *__restrict__ dinv, double2 *__restrict__ pinv,
+                                   const SolveParams *__restrict__ sp) {
     const int64_t tot = ((int64_t)n + ngn) * R;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
         const int r = (int)(t % R);
         const int64_t i = t / R;
-        const double w = c_sp.w32[r];
+        const double w = sp->w32[r];
         if (i < n) {
             const double a = kd[i], b = w * md[i];
             const double s = a * a + b * b;
@@ -683,13 +690,15 @@ struct Work {
     int cycles = 0;
 };
 
-static void free_work(Work &W) {
+// Work buffers come from the stream-ordered allocator: no device-wide synchronisation
+// when they are freed, so solves on different contexts can overlap (mvf_solve_many).
+static void free_work(Ctx *c, Work &W) {
     for (cudaGraphExec_t &g : W.blocks)
         if (g) cudaGraphExecDestroy(g);
-    void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs,
-                 W.pinvs};
+    void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs};
     for (void *q : p)
-        if (q) cudaFree(q);
+        if (q) cudaFreeAsync(q, c->stream);
+    if (W.pinvs) cudaFree(W.pinvs);
     W = Work{};
 }
 
@@ -705,23 +714,23 @@ static int alloc_work(Ctx *c, Work &W, int R, int m) {
     W.nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(152 * 4, ((int64_t)c->nne * R + 511) / 512));
     const size_t nv = (size_t)W.n * R;
     W.vb = nv * sizeof(TV);
-    MVF_CUDA(c, cudaMalloc(&W.V, W.vb * (m + 1)));
-    MVF_CUDA(c, cudaMalloc(&W.Z, W.vb * m));
-    MVF_CUDA(c, cudaMalloc(&W.w, W.vb));
-    MVF_CUDA(c, cudaMalloc(&W.t, (size_t)std::max(c->ngn, 1) * R * sizeof(TV)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.x64, nv * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.b64, nv * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.r64, nv * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.dinv, nv * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.pinv, (size_t)std::max(c->ngn, 1) * R * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.partial, (size_t)W.nblocks * (m + 1) * R * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.hc, (size_t)(m + 1) * R * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.htmp, (size_t)(m + 1) * R * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.nrm, (size_t)R * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.y, (size_t)(m + 1) * R * sizeof(double2)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.kd, (size_t)W.n * sizeof(double)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.md, (size_t)W.n * sizeof(double)));
-    MVF_CUDA(c, cudaMalloc((void **)&W.hs, (size_t)R * sizeof(Hess)));
+    MVF_CUDA(c, cudaMallocAsync(&W.V, W.vb * (m + 1), c->stream));
+    MVF_CUDA(c, cudaMallocAsync(&W.Z, W.vb * m, c->stream));
+    MVF_CUDA(c, cudaMallocAsync(&W.w, W.vb, c->stream));
+    MVF_CUDA(c, cudaMallocAsync(&W.t, (size_t)std::max(c->ngn, 1) * R * sizeof(TV), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.x64, nv * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.b64, nv * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.r64, nv * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.dinv, nv * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.pinv, (size_t)std::max(c->ngn, 1) * R * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.partial, (size_t)W.nblocks * (m + 1) * R * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.hc, (size_t)(m + 1) * R * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.htmp, (size_t)(m + 1) * R * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.nrm, (size_t)R * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.y, (size_t)(m + 1) * R * sizeof(double2), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.kd, (size_t)W.n * sizeof(double), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.md, (size_t)W.n * sizeof(double), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.hs, (size_t)R * sizeof(Hess), c->stream));
     return 0;
 }
 
@@ -740,7 +749,8 @@ static void spmm_variant(Ctx *c, int v, const T *K, const T *M, const TV *x, con
     const int64_t rows_per_block = (threads / 32) * (32 / G);
     const unsigned grid = (unsigned)std::min<int64_t>((c->nne + rows_per_block - 1) / rows_per_block, 152 * 64);
     count_launch();
-#define MVF_SPMM_ARGS <<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32)
+#define MVF_SPMM_ARGS \
+    <<<grid, threads, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, K, M, x, b, y, use_w32, (const SolveParams *)c->d.wsp)
     switch (v) {
         case 1:
             if constexpr (R <= 4) spmm_km_direct<T, TV, R> MVF_SPMM_ARGS;
@@ -990,7 +1000,7 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
     while (R < Rreal) R <<= 1;
     Work W;
     int rc = alloc_work<T>(c, W, R, m);
-    if (rc) { free_work(W); return rc; }
+    if (rc) { free_work(c, W); return rc; }
     // the FP32 inner solve sits inside FP64 refinement, which absorbs the loss of
     // orthogonality of a single pass; the plain FP64 method keeps two passes
     W.passes = std::is_same<T, float>::value ? 1 : 2;
@@ -1000,7 +1010,7 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         std::vector<double> wl(nfs);
         for (int f = 0; f < nfs; ++f)
             wl[f] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f0 + f] : c->omega[f0 + f];
-        if ((rc = patch_invert(c, S, wl.data(), nfs, &W.pinvs))) { free_work(W); return rc; }
+        if ((rc = patch_invert(c, S, wl.data(), nfs, &W.pinvs))) { free_work(c, W); return rc; }
     }
     SolveParams sp{};
     for (int r = 0; r < R; ++r) {
@@ -1008,12 +1018,12 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         sp.omega[r] = c->omega[f];
         sp.w32[r] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
     }
-    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    MVF_CUDA(c, cudaMemcpyAsync(c->d.wsp, &sp, sizeof sp, cudaMemcpyHostToDevice, c->stream));
     count_launch();
     extract_diag<<<grid_for(c->nne), 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.K64, S.M64, W.kd, W.md);
     count_launch();
     build_inverse_diag<<<grid_for(((int64_t)c->nne + c->ngn) * R), 256, 0, c->stream>>>(
-        c->nne, c->ngn, R, W.kd, W.md, S.kphi, S.mphi, S.mabs, W.dinv, W.pinv);
+        c->nne, c->ngn, R, W.kd, W.md, S.kphi, S.mphi, S.mabs, W.dinv, W.pinv, (const SolveParams *)c->d.wsp);
     // gather right-hand sides [f][p][n] -> [n][R]
     if (npol == 2) {
         count_launch();
@@ -1093,7 +1103,7 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         st->rel_residual = std::max(st->rel_residual, worst);
         if (stagnated) st->stagnated = 1;
     }
-    free_work(W);
+    free_work(c, W);
     if (!rc && worst > tol && !stagnated) return MVF_E_NOCONV;
     return rc;
 }
@@ -1147,6 +1157,43 @@ extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mod
     return 0;
 }
 
+// Many independent models at once: host threads take contexts from a queue (largest
+// systems first) and run mvf_solve on each context's own stream, so the small solves
+// of uneven models overlap on the GPU.  Work buffers are stream-ordered allocations
+// and the solver keeps no state outside the context, so the solves do not serialise.
+extern "C" int mvf_solve_many(mvf_ctx **ctx, int32_t n, double tol, int32_t mode, int32_t max_iters, mvf_stats *st,
+                              int32_t nthreads) {
+    if (!ctx || n < 1 || nthreads < 1) return MVF_E_ARG;
+    for (int i = 0; i < n; ++i)
+        if (!ctx[i]) return MVF_E_ARG;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        return (int64_t)ctx[a]->c.nne * ctx[a]->c.nfreq > (int64_t)ctx[b]->c.nne * ctx[b]->c.nfreq;
+    });
+    std::vector<int> rc(n, 0);
+    std::atomic<int> next{0};
+#pragma omp parallel num_threads(nthreads)
+    {
+        for (;;) {
+            const int k = next.fetch_add(1);
+            if (k >= n) break;
+            const int i = order[k];
+            if (cudaSetDevice(ctx[i]->c.device) != cudaSuccess) {
+                rc[i] = MVF_E_CUDA;
+                continue;
+            }
+            rc[i] = mvf_solve(ctx[i], nullptr, tol, mode, max_iters, st ? &st[i] : nullptr);
+        }
+    }
+    int noconv = 0;
+    for (int i = 0; i < n; ++i) {
+        if (rc[i] == MVF_E_NOCONV) noconv = 1;
+        else if (rc[i]) return rc[i];
+    }
+    return noconv ? MVF_E_NOCONV : 0;
+}
+
 extern "C" int64_t mvf_kernel_launches(void) { return launch_counter().load(); }
 
 extern "C" int mvf_set_guess(mvf_ctx *xc, const double *x0) {
@@ -1189,7 +1236,7 @@ extern "C" int mvf_spmm_variant(mvf_ctx *xc, int32_t f, int32_t variant, int32_t
         sp.omega[r] = c->omega[f];
         sp.w32[r] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
     }
-    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    MVF_CUDA(c, cudaMemcpyAsync(c->d.wsp, &sp, sizeof sp, cudaMemcpyHostToDevice, c->stream));
     const size_t nv = (size_t)c->nne * R;
     if (fp64) {
         double2 *dx, *dy;
@@ -1238,7 +1285,7 @@ extern "C" int mvf_profile_spmm(mvf_ctx *xc, int32_t f, int32_t reps, double *se
         sp.omega[r] = c->omega[ff];
         sp.w32[r] = (double)(float)c->omega[ff];
     }
-    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    MVF_CUDA(c, cudaMemcpyAsync(c->d.wsp, &sp, sizeof sp, cudaMemcpyHostToDevice, c->stream));
     float2 *x, *y;
     const size_t nb = (size_t)c->nne * R * sizeof(float2);
     MVF_CUDA(c, cudaMalloc((void **)&x, nb));
@@ -1277,7 +1324,7 @@ extern "C" int mvf_spmv(mvf_ctx *xc, int32_t f, const double *x, double *y) {
     SolveParams sp{};
     sp.omega[0] = sp.omega[1] = c->omega[f];
     sp.w32[0] = sp.w32[1] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
-    MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_sp, &sp, sizeof sp, 0, cudaMemcpyHostToDevice, c->stream));
+    MVF_CUDA(c, cudaMemcpyAsync(c->d.wsp, &sp, sizeof sp, cudaMemcpyHostToDevice, c->stream));
     double2 *dx, *dy, *tx, *ty;
     const size_t nb = (size_t)c->nne * 2 * sizeof(double2);
     MVF_CUDA(c, cudaMalloc((void **)&dx, nb));

@@ -1,8 +1,11 @@
-"""SOLUTION.OUT writer: the layout of the reference's ``write_solution``
-(solution.f90:71-205) for the whole-volume case (``inner == 0``), fed by
-:meth:`movfem_gb300.api.MTProblem.node_fields`.
+"""Output writers in the reference's layouts.
 
-Per frequency block:
+SOLUTION.OUT: ``write_solution`` (solution.f90:71-205), whole-volume case
+(``inner == 0``), fed by :meth:`movfem_gb300.api.MTProblem.node_fields`.
+RECEIVER.OUT: ``write_receiver_data`` (receiver_data.f90:25-67), fed by
+:meth:`movfem_gb300.api.MTProblem.impedance` with ``with_fields=True``.
+
+SOLUTION.OUT, per frequency:
   * a list-directed header line ``vector-fem solution: <nf>``;
   * a '(24A15)' title line and one '(24es20.5)' record per node: Re/Im of E_x, E_y,
     E_z, then B_x, B_y, B_z (the reference prints H with the label B and unit factor 1),
@@ -63,6 +66,56 @@ def solution_block(nf: int, E: np.ndarray, H: np.ndarray, Z: np.ndarray, rho: np
     for ip in range(rho.shape[0]):
         out.append("".join(fw(v) for v in list(rho[ip]) + list(phi[ip])))
     return "\n".join(out) + "\n"
+
+
+def _ld(*vals) -> str:
+    """A list-directed record.  Its exact spacing is compiler-specific: integers in 12
+    columns and reals with 17 significant digits in 25 columns (gfortran's widths for
+    default integers and REAL(8)), after one leading blank."""
+    parts = []
+    for v in vals:
+        if isinstance(v, (int, np.integer)):
+            parts.append(f"{int(v):12d}")
+        elif isinstance(v, str):
+            parts.append(v)
+        else:
+            parts.append(f"{float(v):25.16E}")
+    return " " + "".join(parts)
+
+
+def receiver_block(nf: int, rx: np.ndarray, E, H, Z, rho, phi) -> str:
+    """One frequency's RECEIVER.OUT block (after the coordinate header): rx [nrx, 2]
+    (x, y); E, H [nrx, 2, 3] complex; Z [nrx, 4]; rho, phi [nrx, 4]."""
+    out = [f"{nf:5d} " + "".join(t.rjust(15) for t in ["x", "y"] + _TITLE_E)]
+    for i in range(rx.shape[0]):
+        vals = [rx[i, 0], rx[i, 1]]
+        for p in range(2):
+            for a in range(3):
+                vals += [E[i, p, a].real, E[i, p, a].imag]
+            for a in range(3):
+                vals += [H[i, p, a].real, H[i, p, a].imag]
+        out.append("".join(es(v) for v in vals))
+    out.append(f"{nf:5d} " + "".join(t.rjust(15) for t in ["x", "y"] + _TITLE_Z))
+    for i in range(rx.shape[0]):
+        out.append("".join(es(v) for v in [rx[i, 0], rx[i, 1]] + [w for k in range(4) for w in (Z[i, k].real,
+                                                                                               Z[i, k].imag)]))
+    out.append(f"{nf:5d} " + "".join(t.rjust(15) for t in ["x", "y"] + _TITLE_R))
+    for i in range(rx.shape[0]):
+        out.append("".join(fw(v) for v in [rx[i, 0], rx[i, 1]] + list(rho[i]) + list(phi[i])))
+    return "\n".join(out) + "\n"
+
+
+def write_receivers(path: str, rx: np.ndarray, rz: np.ndarray, E, H, Z, rho, phi) -> None:
+    """RECEIVER.OUT for every frequency (leading axis of E, H, Z, rho, phi); rx [nrx, 2],
+    rz [nrx] the receivers' heights."""
+    nf = E.shape[0]
+    with open(path, "w") as fh:
+        fh.write(_ld("----------------rx coords-----------------------") + "\n")
+        fh.write(_ld(rx.shape[0], 2, nf) + "\n")
+        for i in range(rx.shape[0]):
+            fh.write(_ld(rx[i, 0], rx[i, 1], rz[i]) + "\n")
+        for f in range(nf):
+            fh.write(receiver_block(f + 1, rx, E[f], H[f], Z[f], rho[f], phi[f]))
 
 
 def write_solution(path: str, E, H, Z, rho, phi) -> None:

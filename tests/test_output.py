@@ -41,3 +41,25 @@ def test_block_layout_and_round_trip():
     rrec = lines[-1]
     np.testing.assert_allclose([float(rrec[20 * i:20 * i + 20]) for i in range(8)],
                                list(rho[-1]) + list(phi[-1]), atol=1e-5)
+
+
+def test_receiver_file_layout(tmp_path):
+    rng = np.random.Generator(np.random.PCG64(4))
+    nf, nrx = 2, 3
+    rx = rng.uniform(0, 1000, size=(nrx, 2))
+    E = rng.normal(size=(nf, nrx, 2, 3)) + 1j * rng.normal(size=(nf, nrx, 2, 3))
+    H = rng.normal(size=(nf, nrx, 2, 3)) + 1j * rng.normal(size=(nf, nrx, 2, 3))
+    Z = rng.normal(size=(nf, nrx, 4)) + 1j * rng.normal(size=(nf, nrx, 4))
+    rho = rng.uniform(0, 10, size=(nf, nrx, 4))
+    phi = rng.uniform(-90, 90, size=(nf, nrx, 4))
+    path = tmp_path / "RECEIVER.OUT"
+    output.write_receivers(str(path), rx, np.zeros(nrx), E, H, Z, rho, phi)
+    lines = path.read_text().splitlines()
+    assert len(lines) == 2 + nrx + nf * 3 * (1 + nrx)
+    head = lines[2 + nrx]
+    assert head.startswith("    1 ") and len(head) == 6 + 26 * 15
+    rec = lines[3 + nrx]
+    assert len(rec) == 26 * 20
+    assert abs(float(rec[:20]) - rx[0, 0]) < 1e-3 * max(1.0, abs(rx[0, 0]))
+    assert abs(float(rec[40:60]) - E[0, 0, 0, 0].real) < 1e-5 * max(1.0, abs(E[0, 0, 0, 0].real))
+    assert lines[-1 - nrx].startswith("    2 ") and len(lines[-1]) == 10 * 20
