@@ -165,6 +165,13 @@ int mvf_spmv(mvf_ctx *ctx, int32_t f, const double *x, double *y);
 int mvf_profile_spmm(mvf_ctx *ctx, int32_t f, int32_t reps, double *sec_per_launch, int64_t *bytes);
 int64_t mvf_kernel_launches(void);
 
+/* Measurement hook (no reference counterpart): average device time of one vertex-patch
+ * preconditioner application (36/54-DOF elements; 8 colour launches, 2 right-hand
+ * sides, complex FP64) with frequency f's inverses, and its algorithmic bytes
+ * (inverse entries x 16 B + patch gathers/scatters + zeroing).  MVF_E_UNSUPPORTED for
+ * 12-DOF elements. */
+int mvf_profile_patch(mvf_ctx *ctx, int32_t f, int32_t reps, double *sec_per_apply, int64_t *bytes);
+
 /* Autotuner record (no reference counterpart): the first K/M SpMM of each precision
  * and batch width on a context times every kernel variant on the real operands and
  * keeps the fastest; this returns "fp32 R=2: chunked 227.1 us, direct 173.9 us, ...

@@ -113,7 +113,7 @@ struct Ctx {
     int64_t ke_count = 0;
     // vertex patches
     bool use_patches = false;
-    int64_t npatch = 0, patch_entries = 0;
+    int64_t npatch = 0, patch_entries = 0, patch_dofs = 0;  // patches, sum P^2, sum P
     int patch_max = 0;
     std::vector<int64_t> pcolor_off;
     // SpMM variant chosen by timing, per [FP64?][log2 R]; -1 = not tuned yet
@@ -122,12 +122,21 @@ struct Ctx {
     std::string spmm_note;
 };
 
-// process-wide count of the library's kernel launches
+// process-wide count of the library's kernel launches.  While a thread captures a
+// CUDA graph its launches go to that thread's capture tally instead; the graph's
+// launches are added to the process count each time it is replayed.
 inline std::atomic<int64_t> &launch_counter() {
     static std::atomic<int64_t> n{0};
     return n;
 }
-inline void count_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
+inline int64_t *&capture_tally() {
+    static thread_local int64_t *t = nullptr;
+    return t;
+}
+inline void count_launch() {
+    if (int64_t *t = capture_tally()) ++*t;
+    else launch_counter().fetch_add(1, std::memory_order_relaxed);
+}
 
 int fail(Ctx *c, int code, const std::string &msg);
 int cuda_fail(Ctx *c, cudaError_t e, const char *what);

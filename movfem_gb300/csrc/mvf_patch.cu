@@ -88,6 +88,7 @@ int patch_setup(Ctx *c) {
     c->npatch = np;
     c->patch_max = pmax;
     c->patch_entries = ioff[np];
+    c->patch_dofs = ptr[np];
     MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_ptr, (np + 1) * sizeof(int64_t)));
     MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_dof, std::max<int64_t>(ptr[np], 1) * sizeof(int32_t)));
     MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_ioff, (np + 1) * sizeof(int64_t)));
@@ -293,3 +294,50 @@ void patch_apply(Ctx *c, const double2 *inv, int R, int npol, int nfi, const dou
 }
 
 }  // namespace mvf
+
+using namespace mvf;
+
+// Measurement hook: one preconditioner application (memset + 8 colour launches) of
+// frequency f's patch inverses on 2 right-hand sides in complex FP64, timed with CUDA
+// events on the library's stream.  Algorithmic bytes per application: the inverses
+// (16 B per entry), each patch's gather of r and scatter of z, and the zeroing of z.
+extern "C" int mvf_profile_patch(mvf_ctx *xc, int32_t f, int32_t reps, double *sec_per_apply, int64_t *bytes) {
+    if (!xc || !sec_per_apply || reps < 1) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
+    if (!c->use_patches) return fail(c, MVF_E_UNSUPPORTED, "vertex patches serve the 36/54-DOF elements only");
+    if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
+    const MatrixSet *S = nullptr;
+    for (const MatrixSet &s : c->sets)
+        if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
+    const double w = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
+    double2 *inv = nullptr;
+    if (int rc = patch_invert(c, *S, &w, 1, &inv)) return rc;
+    const int R = 2;
+    const size_t vb = (size_t)c->nne * R * sizeof(double2);
+    double2 *r = nullptr, *z = nullptr;
+    cudaError_t e = cudaMalloc((void **)&r, vb);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&z, vb);
+    if (e == cudaSuccess) e = cudaMemsetAsync(r, 0, vb, c->stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = 0.f;
+    if (e == cudaSuccess) {
+        patch_apply(c, inv, R, 2, 1, r, z);  // warm
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, c->stream);
+        for (int i = 0; i < reps; ++i) patch_apply(c, inv, R, 2, 1, r, z);
+        cudaEventRecord(e1, c->stream);
+        e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    cudaFree(r);
+    cudaFree(z);
+    cudaFree(inv);
+    if (e != cudaSuccess) return cuda_fail(c, e, "patch profile");
+    *sec_per_apply = ms * 1e-3 / reps;
+    if (bytes) *bytes = c->patch_entries * 16 + 2 * c->patch_dofs * R * 16 + (int64_t)c->nne * R * 16;
+    return 0;
+}

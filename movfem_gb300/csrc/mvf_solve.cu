@@ -682,6 +682,7 @@ struct Work {
     Hess *hs = nullptr;
     size_t vb = 0;
     double2 *pinvs = nullptr;  // vertex-patch inverses, one set per frequency
+    double2 *xbest = nullptr;  // iterate with the lowest true residual so far
     int npol = 2, nfi = 1;
     // captured blocks of Arnoldi steps (see fgmres_cycle)
     static constexpr int GCH = 10, MAXB = 8;
@@ -695,7 +696,8 @@ struct Work {
 static void free_work(Ctx *c, Work &W) {
     for (cudaGraphExec_t &g : W.blocks)
         if (g) cudaGraphExecDestroy(g);
-    void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs};
+    void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs,
+                 W.xbest};
     for (void *q : p)
         if (q) cudaFreeAsync(q, c->stream);
     if (W.pinvs) cudaFree(W.pinvs);
@@ -927,14 +929,14 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
         bool done = false;
         if (W.cycles > 0 && kb < Work::MAXB && k % Work::GCH == 0) {
             if (!W.blocks[kb]) {
-                const int64_t c0 = launch_counter().load();
+                int64_t nk = 0;
                 cudaGraph_t g = nullptr;
                 if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
                     int rc = 0;
+                    capture_tally() = &nk;  // counted at each replay instead
                     for (int kk = k; kk < k1 && !rc; ++kk) rc = step(kk);
+                    capture_tally() = nullptr;
                     const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-                    const int64_t nk = launch_counter().load() - c0;
-                    launch_counter().fetch_sub(nk);  // counted again at each replay
                     if (e == cudaSuccess && !rc && g && cudaGraphInstantiate(&W.blocks[kb], g, 0) == cudaSuccess)
                         W.block_launches[kb] = nk;
                     else
@@ -1060,13 +1062,28 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
     int iters = 0, outer = 0;
     const bool mixed = std::is_same<T, float>::value;
     double worst = 1.0;
-    bool stagnated = false;
+    bool stagnated = false, have_best = false;
+    double best = HUGE_VAL;
     std::vector<double> hist;
     while (true) {
         if ((rc = residual_norms(c, W, S, rel, bn))) break;
         worst = 0;
         for (int r = 0; r < Rreal; ++r) worst = std::max(worst, rel[r]);
         hist.push_back(worst);
+        // keep the best iterate; a refinement step that raises the true residual
+        // tenfold above it means the inner solves have stopped helping (near-singular
+        // air block): return the best iterate instead
+        const size_t xb = (size_t)W.n * R * sizeof(double2);
+        if (worst < best) {
+            best = worst;
+            if (worst > tol && iters < max_iters) {
+                if (!W.xbest) MVF_CUDA(c, cudaMallocAsync((void **)&W.xbest, xb, c->stream));
+                MVF_CUDA(c, cudaMemcpyAsync(W.xbest, W.x64, xb, cudaMemcpyDeviceToDevice, c->stream));
+                have_best = true;
+            }
+        } else if (have_best && worst > 10.0 * best) {
+            break;
+        }
         if (worst <= tol || iters >= max_iters) break;
         // Residual floor: without a Dirichlet constraint on them, gradients of nodal
         // functions inside the air (Re(sigma) = 0) are in the kernel of A, and the
@@ -1087,6 +1104,12 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         cast_vec<TV><<<grid_for((int64_t)W.n * R), 256, 0, c->stream>>>((int64_t)W.n * R, W.r64, stage, 1.0);
         const double inner_tol = mixed ? std::max(tol / std::max(worst, 1e-300), 2e-5) : tol / std::max(worst, 1e-300);
         if ((rc = fgmres_cycle<T>(c, W, S, stage, W.x64, inner_tol, iters, est))) break;
+    }
+    if (!rc && have_best && worst > best) {
+        // the last refinement steps made things worse: hand back the best iterate
+        MVF_CUDA(c, cudaMemcpyAsync(W.x64, W.xbest, (size_t)W.n * R * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                    c->stream));
+        worst = best;
     }
     if (!rc) {
         if (npol == 2) {
