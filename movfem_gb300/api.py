@@ -57,7 +57,8 @@ EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numb
            "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches", "mvf_spmv_noalloc",
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
-           "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many", "mvf_profile_patch"]
+           "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many", "mvf_profile_patch",
+           "mvf_set_solver"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
                "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params")
 SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
@@ -109,6 +110,7 @@ def load(build: bool = True):
     L.mvf_node_fields.argtypes = [P, P, P, P, P, P]
     L.mvf_solve_many.argtypes = [P, I32, D, I32, I32, P, I32]
     L.mvf_profile_patch.argtypes = [P, I32, I32, P, P]
+    L.mvf_set_solver.argtypes = [P, I32, I32]
     L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
     L.mvf_net_destroy.argtypes = [P]
     L.mvf_net_destroy.restype = None
@@ -273,6 +275,10 @@ class MTProblem:
         b = ctypes.c_int64()
         self._chk(self.L.mvf_profile_spmm(self.h, f, reps, ctypes.byref(s), ctypes.byref(b)))
         return {"seconds_per_launch": s.value, "bytes_per_launch": b.value}
+
+    def set_solver(self, restart: int = 0, mixed_passes: int = 0):
+        """FGMRES restart length and mixed-mode Gram-Schmidt passes (0 keeps)."""
+        self._chk(self.L.mvf_set_solver(self.h, restart, mixed_passes))
 
     def profile_patch(self, f: int = 0, reps: int = 5):
         """Seconds and algorithmic bytes of one vertex-patch preconditioner application."""

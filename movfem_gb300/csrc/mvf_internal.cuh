@@ -120,6 +120,8 @@ struct Ctx {
     int spmm_pick[2][6] = {{-1, -1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1, -1}};
     float spmm_us[2][6] = {};
     std::string spmm_note;
+    // FGMRES restart length and Gram-Schmidt passes of the mixed-precision mode
+    int restart = 40, mixed_passes = 1;
 };
 
 // process-wide count of the library's kernel launches.  While a thread captures a

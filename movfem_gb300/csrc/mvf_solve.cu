@@ -1005,7 +1005,7 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
     if (rc) { free_work(c, W); return rc; }
     // the FP32 inner solve sits inside FP64 refinement, which absorbs the loss of
     // orthogonality of a single pass; the plain FP64 method keeps two passes
-    W.passes = std::is_same<T, float>::value ? 1 : 2;
+    W.passes = std::is_same<T, float>::value ? c->mixed_passes : 2;
     W.npol = npol;
     W.nfi = nfs;
     if (c->use_patches) {
@@ -1153,14 +1153,14 @@ extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mod
             // all frequencies of the set and both polarisations in one batch; complex
             // FP32 Krylov vectors, except with the vertex-patch preconditioner of the
             // 36/54-DOF elements, whose air-patch inverses need FP64 vectors
-            int r = c->use_patches ? solve_set<double>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, 40)
-                                   : solve_set<float>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, 40);
+            int r = c->use_patches ? solve_set<double>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, c->restart)
+                                   : solve_set<float>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, c->restart);
             if (r == MVF_E_NOCONV) noconv = 1;
             else if (r) { rc = r; break; }
         } else {
             for (int f = S.first_freq; f < S.first_freq + S.nfreq && !rc; ++f)
                 for (int p = 0; p < 2 && !rc; ++p) {
-                    int r = solve_set<double>(c, S, f, 1, p, 1, tol, max_iters, st, 40);
+                    int r = solve_set<double>(c, S, f, 1, p, 1, tol, max_iters, st, c->restart);
                     if (r == MVF_E_NOCONV) noconv = 1;
                     else if (r) rc = r;
                 }
@@ -1215,6 +1215,16 @@ extern "C" int mvf_solve_many(mvf_ctx **ctx, int32_t n, double tol, int32_t mode
         else if (rc[i]) return rc[i];
     }
     return noconv ? MVF_E_NOCONV : 0;
+}
+
+extern "C" int mvf_set_solver(mvf_ctx *xc, int32_t restart, int32_t mixed_passes) {
+    if (!xc) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (restart != 0 && (restart < 2 || restart > 63)) return fail(c, MVF_E_ARG, "restart must be 2..63");
+    if (mixed_passes != 0 && (mixed_passes < 1 || mixed_passes > 2)) return fail(c, MVF_E_ARG, "passes must be 1 or 2");
+    if (restart) c->restart = restart;
+    if (mixed_passes) c->mixed_passes = mixed_passes;
+    return 0;
 }
 
 extern "C" int64_t mvf_kernel_launches(void) { return launch_counter().load(); }
