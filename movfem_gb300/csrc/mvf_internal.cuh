@@ -121,7 +121,7 @@ struct Ctx {
     float spmm_us[2][6] = {};
     std::string spmm_note;
     // FGMRES restart length and Gram-Schmidt passes of the mixed-precision mode
-    int restart = 40, mixed_passes = 1;
+    int restart = 30, mixed_passes = 1;
 };
 
 // process-wide count of the library's kernel launches.  While a thread captures a
