@@ -133,9 +133,11 @@ int mvf_element_matrices(const mvf_ctx *ctx, int64_t e0, int64_t count, int32_t 
 int mvf_solve(mvf_ctx *ctx, double *rhs_inout, double tol, int32_t mode, int32_t max_iters, mvf_stats *st);
 
 /* Solver settings of a context (no counterpart in the reference): FGMRES restart
- * length (2..63, default 30) and Gram-Schmidt passes of the mixed mode (1 or 2,
- * default 1).  0 keeps a setting. */
-int mvf_set_solver(mvf_ctx *ctx, int32_t restart, int32_t mixed_passes);
+ * length (2..63, default 30), Gram-Schmidt passes of the mixed mode (1 or 2,
+ * default 1), and the arithmetic of the vertex-patch preconditioner of the 36/54-DOF
+ * elements: 1 FP64, 2 float-float on the FP32 pipe (default; falls back to FP64 when
+ * an inverse entry does not fit two FP32 halves).  0 keeps a setting. */
+int mvf_set_solver(mvf_ctx *ctx, int32_t restart, int32_t mixed_passes, int32_t patch_precision);
 
 /* Solve n independent contexts (models of any size) concurrently: nthreads host
  * threads take contexts from a queue, largest first, and run mvf_solve (with the

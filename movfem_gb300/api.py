@@ -110,7 +110,7 @@ def load(build: bool = True):
     L.mvf_node_fields.argtypes = [P, P, P, P, P, P]
     L.mvf_solve_many.argtypes = [P, I32, D, I32, I32, P, I32]
     L.mvf_profile_patch.argtypes = [P, I32, I32, P, P]
-    L.mvf_set_solver.argtypes = [P, I32, I32]
+    L.mvf_set_solver.argtypes = [P, I32, I32, I32]
     L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
     L.mvf_net_destroy.argtypes = [P]
     L.mvf_net_destroy.restype = None
@@ -276,9 +276,10 @@ class MTProblem:
         self._chk(self.L.mvf_profile_spmm(self.h, f, reps, ctypes.byref(s), ctypes.byref(b)))
         return {"seconds_per_launch": s.value, "bytes_per_launch": b.value}
 
-    def set_solver(self, restart: int = 0, mixed_passes: int = 0):
-        """FGMRES restart length and mixed-mode Gram-Schmidt passes (0 keeps)."""
-        self._chk(self.L.mvf_set_solver(self.h, restart, mixed_passes))
+    def set_solver(self, restart: int = 0, mixed_passes: int = 0, patch_precision: int = 0):
+        """FGMRES restart length, mixed-mode Gram-Schmidt passes and the patch
+        preconditioner's arithmetic (1 FP64, 2 float-float); 0 keeps a setting."""
+        self._chk(self.L.mvf_set_solver(self.h, restart, mixed_passes, patch_precision))
 
     def profile_patch(self, f: int = 0, reps: int = 5):
         """Seconds and algorithmic bytes of one vertex-patch preconditioner application."""

@@ -122,6 +122,9 @@ struct Ctx {
     std::string spmm_note;
     // FGMRES restart length and Gram-Schmidt passes of the mixed-precision mode
     int restart = 30, mixed_passes = 1;
+    // vertex-patch application arithmetic: 1 FP64, 2 float-float on the FP32 pipe; and
+    // whether the inverses of the last inversion were split into FP32 halves
+    int patch_precision = 2, patch_inv_split = 0;
 };
 
 // process-wide count of the library's kernel launches.  While a thread captures a

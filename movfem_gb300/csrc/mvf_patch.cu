@@ -240,6 +240,89 @@ __global__ void __launch_bounds__(128) patch_apply_kernel(int64_t p0, int64_t p1
     }
 }
 
+// ---- float-float application ---------------------------------------------------
+// GB300 runs FP64 at a small fraction of its FP32 rate, and the FP64 application above
+// is bound by the FP64 pipe.  Here every inverse entry is held as an unevaluated sum
+// hi + lo of two FP32 numbers (same 16 bytes per complex entry), the right-hand sides
+// likewise, and the products and sums run in float-float arithmetic on the FP32 pipe
+// (Dekker/Knuth error-free transformations: a product's rounding error by FMA, a
+// sum's by TwoSum), about 44 significant bits, against 24 for plain FP32 -- enough for
+// inverses whose air-gradient components dwarf the rest.
+
+// s (hi, lo) += a * b, each operand split hi + lo
+__device__ __forceinline__ void ff_mac(float &sh, float &sl, float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, fmaf(al, bh, e));
+    const float t = sh + p;
+    const float bb = t - sh;
+    const float err = (sh - (t - bb)) + (p - bb);
+    const float lo = sl + e + err;
+    sh = t + lo;
+    sl = lo - (sh - t);
+}
+
+// 1 in *bad when an entry cannot be split into FP32 halves without overflow or
+// underflow (then the FP64 application is used)
+__global__ void split_check(int64_t n, const double2 *__restrict__ inv, int *__restrict__ bad) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = inv[i];
+        const double m = fmax(fabs(v.x), fabs(v.y));
+        if (!(m < 1e37) || (m != 0.0 && m < 1e-30)) atomicOr(bad, 1);
+    }
+}
+
+// in place: double2 (re, im) -> float4 (re_hi, im_hi, re_lo, im_lo), same 16 bytes
+__global__ void split_inverses(int64_t n, double2 *__restrict__ inv) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = inv[i];
+        const float xh = __double2float_rn(v.x), yh = __double2float_rn(v.y);
+        const float xl = __double2float_rn(v.x - (double)xh), yl = __double2float_rn(v.y - (double)yh);
+        reinterpret_cast<float4 *>(inv)[i] = make_float4(xh, yh, xl, yl);
+    }
+}
+
+template <class TV>
+__global__ void __launch_bounds__(128) patch_apply_ff_kernel(int64_t p0, int64_t p1, const int64_t *__restrict__ pptr,
+                                                             const int32_t *__restrict__ pdof,
+                                                             const int64_t *__restrict__ ioff,
+                                                             const float4 *__restrict__ inv, int64_t fstride, int R,
+                                                             int npol, int nfi, const TV *__restrict__ r,
+                                                             TV *__restrict__ z) {
+    extern __shared__ float4 rsf[];  // [P][R]: (re_hi, im_hi, re_lo, im_lo)
+    for (int64_t p = p0 + blockIdx.x; p < p1; p += gridDim.x) {
+        const int64_t b0 = pptr[p];
+        const int P = (int)(pptr[p + 1] - b0);
+        for (int t = threadIdx.x; t < P * R; t += blockDim.x) {
+            const int i = t / R, q = t % R;
+            const TV v = r[(int64_t)pdof[b0 + i] * R + q];
+            const double vx = v.x, vy = v.y;
+            const float xh = __double2float_rn(vx), yh = __double2float_rn(vy);
+            rsf[t] = make_float4(xh, yh, __double2float_rn(vx - (double)xh), __double2float_rn(vy - (double)yh));
+        }
+        __syncthreads();
+        const float4 *A = inv + ioff[p];
+        for (int t = threadIdx.x; t < P * R; t += blockDim.x) {
+            const int i = t / R, q = t % R;
+            const float4 *Ai = A + (int64_t)min(q / npol, nfi - 1) * fstride + (int64_t)i * P;
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+            for (int j = 0; j < P; ++j) {
+                const float4 a = Ai[j];
+                const float4 x = rsf[j * R + q];
+                // (a.re + i a.im)(x.re + i x.im)
+                ff_mac(rh, rl, a.x, a.z, x.x, x.z);
+                ff_mac(rh, rl, -a.y, -a.w, x.y, x.w);
+                ff_mac(ih, il, a.x, a.z, x.y, x.w);
+                ff_mac(ih, il, a.y, a.w, x.x, x.z);
+            }
+            TV &o = z[(int64_t)pdof[b0 + i] * R + q];
+            o.x += (decltype(o.x))((double)rh + (double)rl);
+            o.y += (decltype(o.y))((double)ih + (double)il);
+        }
+        __syncthreads();
+    }
+}
+
 // Inverses for the frequencies w[0..nf) of matrix set S: inv[f][entries].
 int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **inv_out) {
     double2 *inv = nullptr;
@@ -262,11 +345,29 @@ int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **
     MVF_CUDA(c, cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     MVF_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(ws);
-    cudaFree(err);
     if (herr) {
+        cudaFree(err);
         cudaFree(inv);
         return fail(c, MVF_E_SINGULAR, "zero pivot in a patch inverse");
     }
+    c->patch_inv_split = 0;
+    if (c->patch_precision == 2) {
+        const int64_t n = ent * nf;
+        const unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
+        int bad = 0;
+        MVF_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+        count_launch();
+        split_check<<<g, 256, 0, c->stream>>>(n, inv, err);
+        MVF_CUDA(c, cudaMemcpyAsync(&bad, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (!bad) {
+            count_launch();
+            split_inverses<<<g, 256, 0, c->stream>>>(n, inv);
+            MVF_CUDA(c, cudaGetLastError());
+            c->patch_inv_split = 1;
+        }
+    }
+    cudaFree(err);
     *inv_out = inv;
     return 0;
 }
@@ -274,15 +375,24 @@ int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **
 template <class TV>
 static void apply_impl(Ctx *c, const double2 *inv, int R, int npol, int nfi, const TV *r, TV *z) {
     cudaMemsetAsync(z, 0, (size_t)c->nne * R * sizeof(TV), c->stream);
-    const size_t sm = (size_t)c->patch_max * R * sizeof(double2);
-    cudaFuncSetAttribute(patch_apply_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const size_t sm = (size_t)c->patch_max * R * 16;  // double2 or float4 per (dof, rhs)
+    const bool ff = c->patch_inv_split != 0;
+    if (ff)
+        cudaFuncSetAttribute(patch_apply_ff_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    else
+        cudaFuncSetAttribute(patch_apply_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     for (int col = 0; col < 8; ++col) {
         const int64_t a = c->pcolor_off[col], b = c->pcolor_off[col + 1];
         if (b <= a) continue;
         const unsigned grid = (unsigned)std::min<int64_t>(b - a, 152 * 16);
         count_launch();
-        patch_apply_kernel<TV><<<grid, 128, sm, c->stream>>>(a, b, c->d.patch_ptr, c->d.patch_dof, c->d.patch_ioff, inv,
-                                                             c->patch_entries, R, npol, nfi, r, z);
+        if (ff)
+            patch_apply_ff_kernel<TV><<<grid, 128, sm, c->stream>>>(a, b, c->d.patch_ptr, c->d.patch_dof,
+                                                                    c->d.patch_ioff, reinterpret_cast<const float4 *>(inv),
+                                                                    c->patch_entries, R, npol, nfi, r, z);
+        else
+            patch_apply_kernel<TV><<<grid, 128, sm, c->stream>>>(a, b, c->d.patch_ptr, c->d.patch_dof, c->d.patch_ioff,
+                                                                 inv, c->patch_entries, R, npol, nfi, r, z);
     }
 }
 

@@ -1065,11 +1065,13 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
     bool stagnated = false, have_best = false;
     double best = HUGE_VAL;
     std::vector<double> hist;
+    std::vector<int> hist_it;  // inner iterations done at each entry of hist
     while (true) {
         if ((rc = residual_norms(c, W, S, rel, bn))) break;
         worst = 0;
         for (int r = 0; r < Rreal; ++r) worst = std::max(worst, rel[r]);
         hist.push_back(worst);
+        hist_it.push_back(iters);
         // keep the best iterate; a refinement step that raises the true residual
         // tenfold above it means the inner solves have stopped helping (near-singular
         // air block): return the best iterate instead
@@ -1090,11 +1092,16 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         // right-hand side carries a component there whenever the nodal sigma's
         // imaginary part differs from i*eps*omega (update_sigma refreshes only part of
         // the nodes, geometry.f90:144-153).  No solver reduces that component; the rest
-        // of the residual, and the surface fields, converge.  Stop once two refinement
-        // steps have not halved the true residual.
-        if (hist.size() >= 3 && worst > 0.5 * hist[hist.size() - 3] && worst < 1e-5) {
-            stagnated = true;
-            break;
+        // of the residual, and the surface fields, converge.  Stop once 80 inner
+        // iterations (at least two refinement steps) have not halved the true residual.
+        if (worst < 1e-5 && hist.size() >= 3) {
+            int j = -1;
+            for (int q = (int)hist.size() - 3; q >= 0; --q)
+                if (hist_it[q] <= iters - 80) { j = q; break; }
+            if (j >= 0 && worst > 0.5 * hist[j]) {
+                stagnated = true;
+                break;
+            }
         }
         ++outer;
         // inner solve on the residual in the Krylov precision, staged in V_m (the cycle
@@ -1217,13 +1224,16 @@ extern "C" int mvf_solve_many(mvf_ctx **ctx, int32_t n, double tol, int32_t mode
     return noconv ? MVF_E_NOCONV : 0;
 }
 
-extern "C" int mvf_set_solver(mvf_ctx *xc, int32_t restart, int32_t mixed_passes) {
+extern "C" int mvf_set_solver(mvf_ctx *xc, int32_t restart, int32_t mixed_passes, int32_t patch_precision) {
     if (!xc) return MVF_E_ARG;
     Ctx *c = &xc->c;
     if (restart != 0 && (restart < 2 || restart > 63)) return fail(c, MVF_E_ARG, "restart must be 2..63");
     if (mixed_passes != 0 && (mixed_passes < 1 || mixed_passes > 2)) return fail(c, MVF_E_ARG, "passes must be 1 or 2");
+    if (patch_precision != 0 && patch_precision != 1 && patch_precision != 2)
+        return fail(c, MVF_E_ARG, "patch precision must be 1 (FP64) or 2 (float-float)");
     if (restart) c->restart = restart;
     if (mixed_passes) c->mixed_passes = mixed_passes;
+    if (patch_precision) c->patch_precision = patch_precision;
     return 0;
 }
 

@@ -298,3 +298,22 @@ def test_solve_many_matches_individual_solves():
         assert s["rel_residual"] <= 1e-10
         zb = q.impedance()[0]
         assert _rel(zb, z) < 1e-7
+
+
+def test_patch_preconditioner_float_float_matches_fp64():
+    """The vertex-patch preconditioner in float-float arithmetic on the FP32 pipe
+    follows the FP64 one: same iteration budget, residuals within 2x, impedances within
+    1e-5 of each other."""
+    m = models.box(20, n=(4, 4, 3), seed=11)
+    w = 2 * math.pi * np.array([0.5])
+    out = {}
+    for prec in (1, 2):
+        p = _problem(m)
+        p.set_solver(patch_precision=prec)
+        p.assemble(w)
+        st = p.solve_device(tol=1e-10, max_iters=120)
+        out[prec] = (st["rel_residual"], p.impedance()[0])
+    r64, z64 = out[1]
+    rff, zff = out[2]
+    assert rff <= 2.0 * r64 + 1e-12
+    assert _rel(zff, z64) < 1e-5
