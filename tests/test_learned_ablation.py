@@ -2,12 +2,11 @@
 kernels on solutions of this solver, then solve held-out models with and without it.
 
 What the network may change is the iteration count; what it may not change is the
-accepted answer.  Asserted: both arms pass the same acceptance (the FP64 true-residual tolerance, or
-the air-kernel floor the solver reports);
-the fitted warm start never starts above the zero start (initial relative residual
-<= 1); training lowers the loss.  The measured iteration ratio is printed.  The one
-measured at scale is recorded with the design notes; the network does not yet
-reduce iterations.
+accepted answer.  Asserted: both arms pass the same acceptance (the FP64 true-residual
+tolerance, or the air-kernel floor the solver reports); the fitted warm start never
+starts above the zero start (initial relative residual <= 1); training lowers the
+loss.  The measured iteration ratio is printed; at this training size the network
+does not yet reduce iterations.
 """
 from __future__ import annotations
 
