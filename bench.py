@@ -216,8 +216,10 @@ def run_ours(args):
         # preconditioner (launch lists in profiles/): one application streams every
         # patch inverse once
         pp = prob.profile_patch(0, reps=5)
+        arith = {1: "FP64", 2: "float-float on the FP32 pipe"}.get(prob.patch_arithmetic(), "none")
         pa = pp["bytes_per_apply"] / pp["seconds_per_apply"] / 1e9
-        roof = {"bound": "hbm", "kernel": "patch_apply_kernel<double2> (8 colour launches)", "achieved": pa,
+        kern = "patch_apply_ff_kernel" if prob.patch_arithmetic() == 2 else "patch_apply_kernel"
+        roof = {"bound": "hbm", "kernel": f"{kern}<double2> (8 colour launches; {arith})", "achieved": pa,
                 "peak": hbm, "unit": "GB/s", "frac": pa / hbm, "peak_kind": peak_kind,
                 "bytes_per_launch": pp["bytes_per_apply"], "us_per_launch": pp["seconds_per_apply"] * 1e6,
                 "traffic": None, "spmm_fp32": spmm_roof}

@@ -135,9 +135,13 @@ int mvf_solve(mvf_ctx *ctx, double *rhs_inout, double tol, int32_t mode, int32_t
 /* Solver settings of a context (no counterpart in the reference): FGMRES restart
  * length (2..63, default 30), Gram-Schmidt passes of the mixed mode (1 or 2,
  * default 1), and the arithmetic of the vertex-patch preconditioner of the 36/54-DOF
- * elements: 1 FP64, 2 float-float on the FP32 pipe (default; falls back to FP64 when
- * an inverse entry does not fit two FP32 halves).  0 keeps a setting. */
+ * elements in the mixed mode: 1 FP64, 2 float-float on the FP32 pipe (default; falls
+ * back to FP64 when a scaled inverse entry does not fit two FP32 halves).  The plain
+ * FP64 mode always applies it in FP64.  0 keeps a setting. */
 int mvf_set_solver(mvf_ctx *ctx, int32_t restart, int32_t mixed_passes, int32_t patch_precision);
+/* Arithmetic the last vertex-patch inversion set up: 0 no patches (12-DOF elements),
+ * 1 FP64, 2 float-float (scaled inverses split into FP32 halves). */
+int32_t mvf_patch_arithmetic(const mvf_ctx *ctx);
 
 /* Solve n independent contexts (models of any size) concurrently: nthreads host
  * threads take contexts from a queue, largest first, and run mvf_solve (with the

@@ -58,9 +58,9 @@ EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numb
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
            "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many", "mvf_profile_patch",
-           "mvf_set_solver"]
+           "mvf_set_solver", "mvf_patch_arithmetic"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
-               "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params")
+               "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params", "mvf_patch_arithmetic")
 SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
 
 
@@ -111,6 +111,8 @@ def load(build: bool = True):
     L.mvf_solve_many.argtypes = [P, I32, D, I32, I32, P, I32]
     L.mvf_profile_patch.argtypes = [P, I32, I32, P, P]
     L.mvf_set_solver.argtypes = [P, I32, I32, I32]
+    L.mvf_patch_arithmetic.argtypes = [P]
+    L.mvf_patch_arithmetic.restype = I32
     L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
     L.mvf_net_destroy.argtypes = [P]
     L.mvf_net_destroy.restype = None
@@ -280,6 +282,10 @@ class MTProblem:
         """FGMRES restart length, mixed-mode Gram-Schmidt passes and the patch
         preconditioner's arithmetic (1 FP64, 2 float-float); 0 keeps a setting."""
         self._chk(self.L.mvf_set_solver(self.h, restart, mixed_passes, patch_precision))
+
+    def patch_arithmetic(self) -> int:
+        """0 no patches, 1 FP64, 2 float-float (as set up by the last inversion)."""
+        return int(self.L.mvf_patch_arithmetic(self.h))
 
     def profile_patch(self, f: int = 0, reps: int = 5):
         """Seconds and algorithmic bytes of one vertex-patch preconditioner application."""

@@ -125,6 +125,7 @@ struct Ctx {
     // vertex-patch application arithmetic: 1 FP64, 2 float-float on the FP32 pipe; and
     // whether the inverses of the last inversion were split into FP32 halves
     int patch_precision = 2, patch_inv_split = 0;
+    int solve_mode = 0;  // mode of the solve in progress (1: plain FP64 throughout)
 };
 
 // process-wide count of the library's kernel launches.  While a thread captures a

@@ -262,23 +262,60 @@ __device__ __forceinline__ void ff_mac(float &sh, float &sl, float ah, float al,
     sl = lo - (sh - t);
 }
 
-// 1 in *bad when an entry cannot be split into FP32 halves without overflow or
-// underflow (then the FP64 application is used)
-__global__ void split_check(int64_t n, const double2 *__restrict__ inv, int *__restrict__ bad) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 v = inv[i];
-        const double m = fmax(fabs(v.x), fabs(v.y));
-        if (!(m < 1e37) || (m != 0.0 && m < 1e-30)) atomicOr(bad, 1);
+// The inverses span many orders of magnitude (air patches, PML stretch), beyond what
+// FP32 halves can hold.  Each patch's inverse is therefore stored scaled symmetrically,
+// S = D^-1 A_v^-1 D^-1 with d_i = sqrt|A_v^-1_ii| (1 where that vanishes), and the
+// application computes z_i = d_i sum_j S_ij (d_j r_j) with d in FP64.  *bad is set when
+// a scaled entry still does not fit two FP32 halves (then the FP64 application is used).
+__device__ __forceinline__ double patch_scale(const double2 *A, int P, int i) {
+    const double2 v = A[(int64_t)i * P + i];
+    const double m = sqrt(hypot(v.x, v.y));
+    return m > 0.0 && m < 1e150 ? m : 1.0;
+}
+
+// one block per (patch, frequency), grid-stride over the patches
+__global__ void scale_check(int64_t np, int nf, const int64_t *__restrict__ pptr, const int64_t *__restrict__ ioff,
+                            int64_t ent, const double2 *__restrict__ inv, int *__restrict__ bad) {
+    for (int64_t pf = blockIdx.x; pf < np * nf; pf += gridDim.x) {
+        const int64_t p = pf % np, f = pf / np;
+        const int P = (int)(pptr[p + 1] - pptr[p]);
+        const double2 *A = inv + f * ent + ioff[p];
+        for (int t = threadIdx.x; t < P * P; t += blockDim.x) {
+            const int i = t / P, j = t % P;
+            const double sc = patch_scale(A, P, i) * patch_scale(A, P, j);
+            const double2 v = A[t];
+            const double m = fmax(fabs(v.x), fabs(v.y)) / sc;
+            if (!(m < 1e30) || (m != 0.0 && m < 1e-25)) atomicOr(bad, 1);
+        }
     }
 }
 
-// in place: double2 (re, im) -> float4 (re_hi, im_hi, re_lo, im_lo), same 16 bytes
-__global__ void split_inverses(int64_t n, double2 *__restrict__ inv) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 v = inv[i];
-        const float xh = __double2float_rn(v.x), yh = __double2float_rn(v.y);
-        const float xl = __double2float_rn(v.x - (double)xh), yl = __double2float_rn(v.y - (double)yh);
-        reinterpret_cast<float4 *>(inv)[i] = make_float4(xh, yh, xl, yl);
+// in place: A_ij (double2) -> S_ij as float4 (re_hi, im_hi, re_lo, im_lo), same 16
+// bytes; d into scale[f][patch dof].  The scales are read from the diagonal before any
+// thread of the block overwrites it.
+__global__ void scale_split(int64_t np, int nf, const int64_t *__restrict__ pptr, const int64_t *__restrict__ ioff,
+                            int64_t ent, int64_t ndof, double2 *__restrict__ inv, double *__restrict__ scale) {
+    extern __shared__ double dsc[];  // [P]
+    for (int64_t pf = blockIdx.x; pf < np * nf; pf += gridDim.x) {
+        const int64_t p = pf % np, f = pf / np;
+        const int64_t b0 = pptr[p];
+        const int P = (int)(pptr[p + 1] - b0);
+        double2 *A = inv + f * ent + ioff[p];
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+            dsc[i] = patch_scale(A, P, i);
+            scale[f * ndof + b0 + i] = dsc[i];
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < P * P; t += blockDim.x) {
+            const int i = t / P, j = t % P;
+            const double sc = dsc[i] * dsc[j];
+            const double2 v = A[t];
+            const double x = v.x / sc, y = v.y / sc;
+            const float xh = __double2float_rn(x), yh = __double2float_rn(y);
+            const float xl = __double2float_rn(x - (double)xh), yl = __double2float_rn(y - (double)yh);
+            reinterpret_cast<float4 *>(A)[t] = make_float4(xh, yh, xl, yl);
+        }
+        __syncthreads();
     }
 }
 
@@ -287,16 +324,18 @@ __global__ void __launch_bounds__(128) patch_apply_ff_kernel(int64_t p0, int64_t
                                                              const int32_t *__restrict__ pdof,
                                                              const int64_t *__restrict__ ioff,
                                                              const float4 *__restrict__ inv, int64_t fstride, int R,
-                                                             int npol, int nfi, const TV *__restrict__ r,
+                                                             int npol, int nfi, const double *__restrict__ scale,
+                                                             int64_t ndof, const TV *__restrict__ r,
                                                              TV *__restrict__ z) {
-    extern __shared__ float4 rsf[];  // [P][R]: (re_hi, im_hi, re_lo, im_lo)
+    extern __shared__ float4 rsf[];  // [P][R]: (re_hi, im_hi, re_lo, im_lo) of d_j r_j
     for (int64_t p = p0 + blockIdx.x; p < p1; p += gridDim.x) {
         const int64_t b0 = pptr[p];
         const int P = (int)(pptr[p + 1] - b0);
         for (int t = threadIdx.x; t < P * R; t += blockDim.x) {
             const int i = t / R, q = t % R;
             const TV v = r[(int64_t)pdof[b0 + i] * R + q];
-            const double vx = v.x, vy = v.y;
+            const double d = scale[(int64_t)min(q / npol, nfi - 1) * ndof + b0 + i];
+            const double vx = d * v.x, vy = d * v.y;
             const float xh = __double2float_rn(vx), yh = __double2float_rn(vy);
             rsf[t] = make_float4(xh, yh, __double2float_rn(vx - (double)xh), __double2float_rn(vy - (double)yh));
         }
@@ -315,9 +354,10 @@ __global__ void __launch_bounds__(128) patch_apply_ff_kernel(int64_t p0, int64_t
                 ff_mac(ih, il, a.x, a.z, x.y, x.w);
                 ff_mac(ih, il, a.y, a.w, x.x, x.z);
             }
+            const double d = scale[(int64_t)min(q / npol, nfi - 1) * ndof + b0 + i];
             TV &o = z[(int64_t)pdof[b0 + i] * R + q];
-            o.x += (decltype(o.x))((double)rh + (double)rl);
-            o.y += (decltype(o.y))((double)ih + (double)il);
+            o.x += (decltype(o.x))(d * ((double)rh + (double)rl));
+            o.y += (decltype(o.y))(d * ((double)ih + (double)il));
         }
         __syncthreads();
     }
@@ -327,7 +367,9 @@ __global__ void __launch_bounds__(128) patch_apply_ff_kernel(int64_t p0, int64_t
 int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **inv_out) {
     double2 *inv = nullptr;
     const int64_t ent = c->patch_entries;
-    MVF_CUDA(c, cudaMalloc((void **)&inv, std::max<int64_t>(ent * nf, 1) * sizeof(double2)));
+    // inverses [nf][entries], then room for the float-float scales [nf][patch dofs]
+    MVF_CUDA(c, cudaMalloc((void **)&inv, std::max<int64_t>(ent * nf, 1) * sizeof(double2) +
+                                              (size_t)nf * c->patch_dofs * sizeof(double)));
     const int grid = (int)std::min<int64_t>(c->npatch, 152 * 8);
     double2 *ws = nullptr;
     int *err = nullptr;
@@ -351,18 +393,19 @@ int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **
         return fail(c, MVF_E_SINGULAR, "zero pivot in a patch inverse");
     }
     c->patch_inv_split = 0;
-    if (c->patch_precision == 2) {
-        const int64_t n = ent * nf;
-        const unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    if (c->patch_precision == 2 && c->solve_mode == 0) {
+        const unsigned g = (unsigned)std::min<int64_t>(c->npatch * nf, 152 * 16);
         int bad = 0;
         MVF_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), c->stream));
         count_launch();
-        split_check<<<g, 256, 0, c->stream>>>(n, inv, err);
+        scale_check<<<g, 256, 0, c->stream>>>(c->npatch, nf, c->d.patch_ptr, c->d.patch_ioff, ent, inv, err);
         MVF_CUDA(c, cudaMemcpyAsync(&bad, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         MVF_CUDA(c, cudaStreamSynchronize(c->stream));
         if (!bad) {
             count_launch();
-            split_inverses<<<g, 256, 0, c->stream>>>(n, inv);
+            scale_split<<<g, 256, (size_t)c->patch_max * sizeof(double), c->stream>>>(
+                c->npatch, nf, c->d.patch_ptr, c->d.patch_ioff, ent, c->patch_dofs, inv,
+                reinterpret_cast<double *>(inv + ent * nf));
             MVF_CUDA(c, cudaGetLastError());
             c->patch_inv_split = 1;
         }
@@ -387,9 +430,10 @@ static void apply_impl(Ctx *c, const double2 *inv, int R, int npol, int nfi, con
         const unsigned grid = (unsigned)std::min<int64_t>(b - a, 152 * 16);
         count_launch();
         if (ff)
-            patch_apply_ff_kernel<TV><<<grid, 128, sm, c->stream>>>(a, b, c->d.patch_ptr, c->d.patch_dof,
-                                                                    c->d.patch_ioff, reinterpret_cast<const float4 *>(inv),
-                                                                    c->patch_entries, R, npol, nfi, r, z);
+            patch_apply_ff_kernel<TV><<<grid, 128, sm, c->stream>>>(
+                a, b, c->d.patch_ptr, c->d.patch_dof, c->d.patch_ioff, reinterpret_cast<const float4 *>(inv),
+                c->patch_entries, R, npol, nfi,
+                reinterpret_cast<const double *>(inv + (int64_t)nfi * c->patch_entries), c->patch_dofs, r, z);
         else
             patch_apply_kernel<TV><<<grid, 128, sm, c->stream>>>(a, b, c->d.patch_ptr, c->d.patch_dof, c->d.patch_ioff,
                                                                  inv, c->patch_entries, R, npol, nfi, r, z);
@@ -422,6 +466,7 @@ extern "C" int mvf_profile_patch(mvf_ctx *xc, int32_t f, int32_t reps, double *s
         if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
     const double w = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
     double2 *inv = nullptr;
+    c->solve_mode = 0;  // the arithmetic of the mixed mode's application
     if (int rc = patch_invert(c, *S, &w, 1, &inv)) return rc;
     const int R = 2;
     const size_t vb = (size_t)c->nne * R * sizeof(double2);
@@ -450,4 +495,9 @@ extern "C" int mvf_profile_patch(mvf_ctx *xc, int32_t f, int32_t reps, double *s
     *sec_per_apply = ms * 1e-3 / reps;
     if (bytes) *bytes = c->patch_entries * 16 + 2 * c->patch_dofs * R * 16 + (int64_t)c->nne * R * 16;
     return 0;
+}
+
+extern "C" int32_t mvf_patch_arithmetic(const mvf_ctx *xc) {
+    if (!xc || !xc->c.use_patches) return 0;
+    return xc->c.patch_inv_split ? 2 : 1;
 }

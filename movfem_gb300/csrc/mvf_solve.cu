@@ -1148,6 +1148,7 @@ extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mod
     if (!c->assembled) return fail(c, MVF_E_STATE, "assemble before solve");
     if (!(tol > 0) || max_iters < 1) return fail(c, MVF_E_ARG, "tol > 0 and max_iters >= 1 required");
     if (st) *st = mvf_stats{};
+    c->solve_mode = mode;  // the plain FP64 mode keeps the patch preconditioner in FP64 too
     const size_t vb = (size_t)c->nfreq * 2 * c->nne * 2 * sizeof(double);
     if (rhs_inout) MVF_CUDA(c, cudaMemcpy(c->d.rhs, rhs_inout, vb, cudaMemcpyHostToDevice));
     cudaEvent_t e0, e1;

@@ -312,6 +312,7 @@ def test_patch_preconditioner_float_float_matches_fp64():
         p.set_solver(patch_precision=prec)
         p.assemble(w)
         st = p.solve_device(tol=1e-10, max_iters=120)
+        assert p.patch_arithmetic() == prec
         out[prec] = (st["rel_residual"], p.impedance()[0])
     r64, z64 = out[1]
     rff, zff = out[2]
