@@ -4,6 +4,8 @@ SOLUTION.OUT: ``write_solution`` (solution.f90:71-205), whole-volume case
 (``inner == 0``), fed by :meth:`movfem_gb300.api.MTProblem.node_fields`.
 RECEIVER.OUT: ``write_receiver_data`` (receiver_data.f90:25-67), fed by
 :meth:`movfem_gb300.api.MTProblem.impedance` with ``with_fields=True``.
+SURFACE.OUT: ``write_surface_data`` (receiver_data.f90:69-109) on the surface nodes
+that ``sur_data`` selects, fed by ``node_fields``.
 
 SOLUTION.OUT, per frequency:
   * a list-directed header line ``vector-fem solution: <nf>``;
@@ -123,3 +125,48 @@ def write_solution(path: str, E, H, Z, rho, phi) -> None:
     with open(path, "w") as fh:
         for f in range(E.shape[0]):
             fh.write(solution_block(f + 1, E[f], H[f], Z[f], rho[f], phi[f]))
+
+
+def surface_nodes(m) -> np.ndarray:
+    """Node ids of the inner-grid surface in sur_data's order (receiver_data.f90:135-168):
+    j outer, i inner, over the nodes inside the extension cells, at the node layer
+    below the top padding and air layers."""
+    s = m.nord - 1
+    i1, i2 = m.nextd * s, m.nnx - 1 - m.nextd * s
+    j1, j2 = m.nextd * s, m.nny - 1 - m.nextd * s
+    k = m.nnz - 1 - (m.nzl_top + m.nzl_air) * s
+    return np.array([(i * m.nny + j) * m.nnz + k for j in range(j1, j2 + 1) for i in range(i1, i2 + 1)],
+                    dtype=np.int64)
+
+
+def write_surface(path: str, m, E, H, Z, rho, phi) -> None:
+    """SURFACE.OUT (write_surface_data, receiver_data.f90:69-109) from the full-volume
+    fields of :meth:`movfem_gb300.api.MTProblem.node_fields` (leading axis: frequency)."""
+    ids = surface_nodes(m)
+    s = m.nord - 1
+    xs = np.asarray(m.xp)[m.nextd * s: m.nnx - m.nextd * s]
+    ys = np.asarray(m.yp)[m.nextd * s: m.nny - m.nextd * s]
+    nf = E.shape[0]
+    with open(path, "w") as fh:
+        fh.write(_ld("-----------------surface coords----------------") + "\n")
+        fh.write(_ld(xs.size, ys.size, ids.size, 2, nf) + "\n")
+        fh.write(_ld(*xs) + "\n")
+        fh.write(_ld(*ys) + "\n")
+        fh.write(_ld(*np.asarray(m.zp)[ids]) + "\n")
+        for f in range(nf):
+            out = [f"{f + 1:5d} " + "".join(t.rjust(15) for t in _TITLE_E)]
+            for n in ids:
+                vals = []
+                for p in range(2):
+                    for a in range(3):
+                        vals += [E[f, n, p, a].real, E[f, n, p, a].imag]
+                    for a in range(3):
+                        vals += [H[f, n, p, a].real, H[f, n, p, a].imag]
+                out.append("".join(es(v) for v in vals))
+            out.append(f"{f + 1:5d} " + "".join(t.rjust(15) for t in _TITLE_Z))
+            for n in ids:
+                out.append("".join(es(v) for i in range(4) for v in (Z[f, n, i].real, Z[f, n, i].imag)))
+            out.append(f"{f + 1:5d} " + "".join(t.rjust(15) for t in _TITLE_R))
+            for n in ids:
+                out.append("".join(fw(v) for v in list(rho[f, n]) + list(phi[f, n])))
+            fh.write("\n".join(out) + "\n")

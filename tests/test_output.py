@@ -63,3 +63,26 @@ def test_receiver_file_layout(tmp_path):
     assert abs(float(rec[:20]) - rx[0, 0]) < 1e-3 * max(1.0, abs(rx[0, 0]))
     assert abs(float(rec[40:60]) - E[0, 0, 0, 0].real) < 1e-5 * max(1.0, abs(E[0, 0, 0, 0].real))
     assert lines[-1 - nrx].startswith("    2 ") and len(lines[-1]) == 10 * 20
+
+
+def test_surface_file_layout(tmp_path):
+    from movfem_gb300 import mesh as M
+    m = M.layered_blocks(3, nodes_per_elem=8, ncx=4, ncy=3, ncz=2, d=100.0, nextd=1, n_air=2, dz_air=100.0,
+                         nfreq=2, fmin=1.0, fmax=10.0, nrx=2)
+    ids = output.surface_nodes(m)
+    # inner grid without the extension cells, at the earth surface
+    assert ids.size == (m.nnx - 2) * (m.nny - 2)
+    assert np.allclose(np.asarray(m.zp)[ids], m.ztop)
+    rng = np.random.Generator(np.random.PCG64(5))
+    nf, npt = 2, m.npt
+    E = rng.normal(size=(nf, npt, 2, 3)) + 0j
+    H = rng.normal(size=(nf, npt, 2, 3)) + 0j
+    Z = rng.normal(size=(nf, npt, 4)) + 0j
+    rho = rng.uniform(0, 10, size=(nf, npt, 4))
+    phi = rng.uniform(-90, 90, size=(nf, npt, 4))
+    path = tmp_path / "SURFACE.OUT"
+    output.write_surface(str(path), m, E, H, Z, rho, phi)
+    lines = path.read_text().splitlines()
+    assert len(lines) == 5 + nf * 3 * (1 + ids.size)
+    rec = lines[6]
+    assert abs(float(rec[:20]) - E[0, ids[0], 0, 0].real) < 1e-5 * max(1.0, abs(E[0, ids[0], 0, 0].real))
