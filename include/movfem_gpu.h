@@ -192,7 +192,8 @@ const char *mvf_spmm_tuning(mvf_ctx *ctx);
 
 /* Parity hook for the autotuner's candidates (no reference counterpart): y = A_f x
  * for R right-hand sides (R a power of two <= 32) with SpMM variant `variant`
- * (0 chunked, 1 direct [R <= 4], 2..5 G = 4/8/16/32 lanes per row [R <= 16]) in FP64
+ * (0 chunked, 1 direct [R <= 4], 2..5 G = 4/8/16/32 lanes per row [R <= 16],
+ * 6 float-float operator of the FP64 Krylov path [fp64 = 1, R <= 8]) in FP64
  * (fp64 = 1: K, M and vectors FP64) or FP32 (K, M, vectors complex64); w is the
  * frequency's omega, rounded to FP32 when the mesh's quirks carry MVF_Q_FP32_CONST,
  * as in assembly.  x, y: host [nne][R] complex. */

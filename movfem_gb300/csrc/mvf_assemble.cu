@@ -685,7 +685,7 @@ static int upload_glist(Ctx *c) {
 
 void free_sets(Ctx *c) {
     for (MatrixSet &S : c->sets) {
-        void *p[] = {S.K64, S.M64, S.K32, S.M32, S.kphi, S.mphi, S.mabs};
+        void *p[] = {S.K64, S.M64, S.K32, S.M32, S.kphi, S.mphi, S.mabs, S.Kff, S.Mff};
         for (void *q : p)
             if (q) cudaFree(q);
     }

@@ -42,6 +42,7 @@ struct OrderTables {
 struct MatrixSet {
     double *K64 = nullptr, *M64 = nullptr;  // [nnz]
     float *K32 = nullptr, *M32 = nullptr;   // [nnz]
+    float2 *Kff = nullptr, *Mff = nullptr;  // [nnz] FP64 values as hi + lo FP32 halves (made on demand)
     double *kphi = nullptr, *mphi = nullptr, *mabs = nullptr;  // gradient-node diagonals [ngn]
     int first_freq = 0, nfreq = 0;          // frequencies that use this set
 };

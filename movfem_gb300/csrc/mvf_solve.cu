@@ -264,6 +264,109 @@ __global__ void __launch_bounds__(256) spmm_km_vec(int32_t n, const int64_t *__r
     }
 }
 
+// ---- float-float K/M SpMM for the FP64 Krylov vectors of the 36/54-DOF systems -------
+// The FP64 SpMM is bound by GB300's FP64 pipe.  Here K and M are held as hi + lo FP32
+// halves (8 bytes a value, as FP64), the Krylov vector is split the same way once per
+// product, and the products and sums run in float-float arithmetic on the FP32 pipe
+// (FMA-exact products, TwoSum), about 44 significant bits.  Only the inner Krylov
+// operator uses it; every true residual stays in FP64.
+
+__device__ __forceinline__ void ffm(float &sh, float &sl, float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, fmaf(al, bh, e));
+    const float t = sh + p;
+    const float bb = t - sh;
+    const float err = (sh - (t - bb)) + (p - bb);
+    const float lo = sl + e + err;
+    sh = t + lo;
+    sl = lo - (sh - t);
+}
+
+__device__ __forceinline__ void ffadd(float &sh, float &sl, float bh, float bl) {
+    const float t = sh + bh;
+    const float bb = t - sh;
+    const float err = (sh - (t - bb)) + (bh - bb);
+    const float lo = sl + bl + err;
+    sh = t + lo;
+    sl = lo - (sh - t);
+}
+
+__global__ void split_values(int64_t n, const double *__restrict__ a, float2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = a[i];
+        const float h = __double2float_rn(v);
+        out[i] = make_float2(h, __double2float_rn(v - (double)h));
+    }
+}
+
+__global__ void split_vector(int64_t n, const double2 *__restrict__ x, float4 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = x[i];
+        const float xh = __double2float_rn(v.x), yh = __double2float_rn(v.y);
+        out[i] = make_float4(xh, yh, __double2float_rn(v.x - (double)xh), __double2float_rn(v.y - (double)yh));
+    }
+}
+
+// y = (K + i w M) x for R right-hand sides, G lanes per row, each lane all R; the
+// group's float-float partial sums meet by xor-shuffles with TwoSum.
+template <int R, int G>
+__global__ void __launch_bounds__(256) spmm_ff(int32_t n, const int64_t *__restrict__ rowptr,
+                                               const int32_t *__restrict__ col, const float2 *__restrict__ K,
+                                               const float2 *__restrict__ M, const float4 *__restrict__ x,
+                                               double2 *__restrict__ y, const SolveParams *__restrict__ sp) {
+    constexpr int RPW = 32 / G;
+    const int lane = threadIdx.x & 31, g = lane / G, j = lane % G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
+        const int64_t row = base + g;
+        int64_t k0 = 0, k1 = 0;
+        if (row < n) {
+            k0 = __ldg(rowptr + row);
+            k1 = __ldg(rowptr + row + 1);
+        }
+        // [r][0..7]: K x re (hi, lo), K x im, M x re, M x im
+        float acc[R][8];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[r][q] = 0.f;
+        for (int64_t k = k0 + j; k < k1; k += G) {
+            const int c = __ldg(col + k);
+            const float2 kv = __ldg(K + k), mv = __ldg(M + k);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float4 xv = __ldg(x + (int64_t)c * R + r);
+                ffm(acc[r][0], acc[r][1], kv.x, kv.y, xv.x, xv.z);
+                ffm(acc[r][2], acc[r][3], kv.x, kv.y, xv.y, xv.w);
+                ffm(acc[r][4], acc[r][5], mv.x, mv.y, xv.x, xv.z);
+                ffm(acc[r][6], acc[r][7], mv.x, mv.y, xv.y, xv.w);
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1)
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+#pragma unroll
+                for (int q = 0; q < 8; q += 2) {
+                    const float bh = __shfl_xor_sync(0xffffffffu, acc[r][q], o);
+                    const float bl = __shfl_xor_sync(0xffffffffu, acc[r][q + 1], o);
+                    ffadd(acc[r][q], acc[r][q + 1], bh, bl);
+                }
+        if (row < n) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (r % G != j) continue;
+                const double w = sp->w32[r];
+                const double kr = (double)acc[r][0] + acc[r][1], ki = (double)acc[r][2] + acc[r][3];
+                const double mr = (double)acc[r][4] + acc[r][5], mi = (double)acc[r][6] + acc[r][7];
+                y[row * R + r] = make_double2(kr - w * mi, ki + w * mr);
+            }
+        }
+    }
+}
+
 // diagonal entries of K and M
 __global__ void extract_diag(int32_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
                              const double *__restrict__ K, const double *__restrict__ M, double *__restrict__ kd,
@@ -683,6 +786,7 @@ struct Work {
     size_t vb = 0;
     double2 *pinvs = nullptr;  // vertex-patch inverses, one set per frequency
     double2 *xbest = nullptr;  // iterate with the lowest true residual so far
+    float4 *xf = nullptr;      // float-float copy of the SpMM input (float-float operator)
     int npol = 2, nfi = 1;
     // captured blocks of Arnoldi steps (see fgmres_cycle)
     static constexpr int GCH = 10, MAXB = 8;
@@ -697,7 +801,7 @@ static void free_work(Ctx *c, Work &W) {
     for (cudaGraphExec_t &g : W.blocks)
         if (g) cudaGraphExecDestroy(g);
     void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs,
-                 W.xbest};
+                 W.xbest, W.xf};
     for (void *q : p)
         if (q) cudaFreeAsync(q, c->stream);
     if (W.pinvs) cudaFree(W.pinvs);
@@ -840,6 +944,37 @@ static void launch_spmm(Ctx *c, int R, const T *K, const T *M, const TV *x, cons
 
 static unsigned grid_for(int64_t n) { return (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 32); }
 
+// float-float operator of the FP64 Krylov path: split x, then y = (K + i w M) x
+static void launch_spmm_ff(Ctx *c, const MatrixSet &S, int R, const double2 *x, double2 *y, float4 *xf) {
+    const int64_t nv = (int64_t)c->nne * R;
+    count_launch();
+    split_vector<<<grid_for(nv), 256, 0, c->stream>>>(nv, x, xf);
+    constexpr int G = 16;
+    const int64_t rows_per_block = 8 * (32 / G);
+    const unsigned grid = (unsigned)std::min<int64_t>((c->nne + rows_per_block - 1) / rows_per_block, 152 * 64);
+    const SolveParams *sp = (const SolveParams *)c->d.wsp;
+    count_launch();
+    switch (R) {
+        case 1: spmm_ff<1, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp); break;
+        case 2: spmm_ff<2, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp); break;
+        case 4: spmm_ff<4, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp); break;
+        default: spmm_ff<8, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp); break;
+    }
+}
+
+// K, M as FP32 halves for the float-float operator (once per matrix set)
+static int ensure_split(Ctx *c, MatrixSet &S) {
+    if (S.Kff) return 0;
+    MVF_CUDA(c, cudaMalloc((void **)&S.Kff, c->nnz * sizeof(float2)));
+    MVF_CUDA(c, cudaMalloc((void **)&S.Mff, c->nnz * sizeof(float2)));
+    count_launch();
+    split_values<<<grid_for(c->nnz), 256, 0, c->stream>>>(c->nnz, S.K64, S.Kff);
+    count_launch();
+    split_values<<<grid_for(c->nnz), 256, 0, c->stream>>>(c->nnz, S.M64, S.Mff);
+    MVF_CUDA(c, cudaGetLastError());
+    return 0;
+}
+
 // Orthogonalise w against V_0..V_{k-1} with W.passes classical Gram-Schmidt passes
 // (FP64 projections), write the projections to W.hc[0..k) and ||w||^2 to W.nrm.
 template <class TV>
@@ -911,7 +1046,14 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
     // one Arnoldi step: z_k = P v_k, w = A z_k, orthogonalise, v_{k+1} = w / ||w||
     auto step = [&](int k) -> int {
         precondition<TV>(c, W, V + k * vs, Z + k * vs);
-        launch_spmm<T, TV>(c, R, K, M, Z + k * vs, (const TV *)nullptr, w, use_w32);
+        bool ff = false;
+        if constexpr (std::is_same<T, double>::value) {
+            if (W.xf) {
+                launch_spmm_ff(c, S, R, Z + k * vs, w, W.xf);
+                ff = true;
+            }
+        }
+        if (!ff) launch_spmm<T, TV>(c, R, K, M, Z + k * vs, (const TV *)nullptr, w, use_w32);
         int rc = cgs2<TV>(c, W, k + 1);
         if (rc) return rc;
         count_launch();
@@ -1013,6 +1155,10 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         for (int f = 0; f < nfs; ++f)
             wl[f] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f0 + f] : c->omega[f0 + f];
         if ((rc = patch_invert(c, S, wl.data(), nfs, &W.pinvs))) { free_work(c, W); return rc; }
+        if (std::is_same<T, double>::value && c->solve_mode == 0 && c->patch_precision == 2 && R <= 8) {
+            MVF_CUDA(c, cudaMallocAsync((void **)&W.xf, (size_t)W.n * R * sizeof(float4), c->stream));
+            if ((rc = ensure_split(c, const_cast<MatrixSet &>(S)))) { free_work(c, W); return rc; }
+        }
     }
     SolveParams sp{};
     for (int r = 0; r < R; ++r) {
@@ -1270,7 +1416,9 @@ extern "C" int mvf_spmm_variant(mvf_ctx *xc, int32_t f, int32_t variant, int32_t
     Ctx *c = &xc->c;
     if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
     if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
-    if (R < 1 || R > MAXR || (R & (R - 1)) || variant < 0 || variant >= SPMM_VARIANTS || !spmm_ok(variant, R))
+    const bool ffv = variant == SPMM_VARIANTS;  // the float-float operator (FP64 vectors, R <= 8)
+    if (R < 1 || R > MAXR || (R & (R - 1)) || variant < 0 || variant > SPMM_VARIANTS ||
+        (!ffv && !spmm_ok(variant, R)) || (ffv && (!fp64 || R > 8)))
         return fail(c, MVF_E_ARG, "bad variant / right-hand-side count");
     const MatrixSet *S = nullptr;
     for (const MatrixSet &s : c->sets)
@@ -1287,7 +1435,16 @@ extern "C" int mvf_spmm_variant(mvf_ctx *xc, int32_t f, int32_t variant, int32_t
         MVF_CUDA(c, cudaMalloc((void **)&dx, nv * sizeof(double2)));
         MVF_CUDA(c, cudaMalloc((void **)&dy, nv * sizeof(double2)));
         MVF_CUDA(c, cudaMemcpyAsync(dx, x, nv * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
-        spmm_dispatch<double, double2>(c, variant, R, S->K64, S->M64, dx, nullptr, dy, 1);
+        if (ffv) {
+            float4 *xf;
+            if (int rc = ensure_split(c, const_cast<MatrixSet &>(*S))) return rc;
+            MVF_CUDA(c, cudaMalloc((void **)&xf, nv * sizeof(float4)));
+            launch_spmm_ff(c, *S, R, dx, dy, xf);
+            MVF_CUDA(c, cudaStreamSynchronize(c->stream));
+            cudaFree(xf);
+        } else {
+            spmm_dispatch<double, double2>(c, variant, R, S->K64, S->M64, dx, nullptr, dy, 1);
+        }
         MVF_CUDA(c, cudaMemcpyAsync(y, dy, nv * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
         MVF_CUDA(c, cudaStreamSynchronize(c->stream));
         cudaFree(dx);

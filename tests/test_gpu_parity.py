@@ -139,6 +139,10 @@ def test_every_spmm_variant_matches_cpu_product(mn):
             assert _rel(y64, ref) < 1e-12, (R, api.SPMM_VARIANTS[v])
             y32 = p.spmm_variant(0, v, False, x)
             assert np.max(np.abs(y32 - ref) / scale) < 2e-6, (R, api.SPMM_VARIANTS[v])
+        if R <= 8:
+            # the float-float operator (FP32 halves of K, M and x; about 44 bits)
+            yff = p.spmm_variant(0, 6, True, x)
+            assert np.max(np.abs(yff - ref) / scale) < 1e-11, R
     assert p.spmm_tuning() == "" or "R=" in p.spmm_tuning()
 
 
