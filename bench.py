@@ -279,6 +279,95 @@ def cpu_baseline(args, m, omega, sig_f, budget_s=20.0):
 
 
 BATCH = "batched-64-uneven"
+MAP = "model-map-lagrangian-96x96x64"
+MAP_METRIC = "grid nodes mapped/s (inner geomodel -> nodal sigma, mu)"
+
+
+def make_map_config(small: bool = False):
+    """The grid of the large Lagrangian stress case (27-node elements, 96x96x64 cells at
+    25 m, 8 padding cells per side, 10 air cells, Gaussian-sum topography of up to
+    +-300 m) and an inner geomodel of one point per core cell (96x96x64 points at the
+    cell centres, following the topography) with a full 6-component anisotropic sigma
+    and three layers.  ``small`` gives the same kind at 8x8x6 cells (the CPU sample)."""
+    rng = np.random.Generator(np.random.PCG64(20261205))
+    n, nz = (8, 6) if small else (96, 64)
+    d = 25.0
+    L = n * d
+    g = [(rng.uniform(0, L), rng.uniform(0, L), rng.uniform(-300, 300), rng.uniform(300, 1500)) for _ in range(5)]
+
+    def topo(x, y):
+        h = np.zeros_like(x, dtype=np.float64)
+        for cx, cy, a, w in g:
+            h = h + a * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * w * w))
+        return np.clip(h, -300.0, 300.0)
+
+    m = M.build_mesh(nodes_per_elem=27, ncx=n, ncy=n, ncz_earth=nz, dx=d, dy=d, dz=d, n_air=10, dz_air=2 * d,
+                     nextd=8, sigma_fn=lambda x, y, dep: 0.01 + 0 * x, omega1=2 * math.pi * 1e-3, topo_fn=topo,
+                     dirichlet=0, gpml_sch=1)
+    gm = M.synthetic_geomodel(20261206, m, spacing=d, depth=nz * d, anisotropic=True, relief=0.0, topo_fn=topo)
+    cfg = {"workload": f"model-map lagrangian-27 {n}x{n}x{nz}+8pad+10air topo+-300m, "
+                       f"{gm.zm.shape[0]}x{gm.zm.shape[1]}x{gm.zm.shape[2]} model points, 6-component sigma",
+           "npt": int(m.npt), "model_points": int(gm.zm.size)}
+    return m, gm, cfg
+
+
+def run_map(args):
+    """One step = one mvf_map_model call: the grid and model copied in, every node
+    mapped, sigma and mu copied out.  ``value`` uses the kernels' device time (CUDA
+    events in the library), ``e2e`` the call's wall time with the host copies."""
+    import torch
+    from movfem_gb300 import api
+    torch.cuda.set_device(0)
+    m, gm, cfg = make_map_config()
+    w = 2 * math.pi * 1e-3
+    for _ in range(args.warmup):
+        api.map_model(m, gm, w, device=0)
+    launches0 = api.kernel_launches()
+    dev, wall = 0.0, 0.0
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.time()
+            sigma, mu, sec = api.map_model(m, gm, w, device=0, timed=True)
+            wall += time.time() - t0
+            dev += sec
+    launches = api.kernel_launches() - launches0
+    npt = m.npt
+    line = {"metric": MAP_METRIC, "value": npt * args.steps / dev, "unit": "nodes/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "replicas", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic seeded grid and geomodel (numpy PCG64)",
+            "config": dict(cfg, l2="inputs larger than L2"),
+            "e2e": {"value": npt * args.steps / wall, "unit": "nodes/s",
+                    "h2d_bytes_per_step": int(8 * (m.nnx + m.nny + npt + gm.zm.size * (1 + gm.sigma.shape[1]))
+                                              + 8 * (gm.xm.size + gm.ym.size)),
+                    "d2h_bytes_per_step": int(sigma.nbytes + mu.nbytes)},
+            "gpu_launches": launches, "clocks": clk.summary(), "roofline": None}
+    line["cpu_baseline"] = None if args.no_cpu else map_cpu_baseline(m, gm, w)
+    print(json.dumps(line))
+
+
+def map_cpu_baseline(m, gm, w):
+    """The oracle (the reference's brute-force scan, one thread) timed on the same
+    geomodel over the small grid of the same kind; its cost per node visit (one scan
+    of every model point) projects the full grid's time."""
+    import oracle
+    ms, _, _ = make_map_config(small=True)
+
+    def visits(mesh):
+        o = mesh.nord - 1
+        ne = (mesh.nx - 2 * mesh.nextd) * (mesh.ny - 2 * mesh.nextd) * (mesh.nz - mesh.nzl_top - mesh.nzl_air
+                                                                         - mesh.nextd + 1)
+        return ne * (o + 1) ** 3
+
+    t0 = time.time()
+    oracle.map_model(ms, gm, w)
+    dt = time.time() - t0
+    per_visit = dt / visits(ms)
+    full = per_visit * visits(m)
+    return {"value": m.npt / full, "unit": "nodes/s", "cores": 1, "kind": "port",
+            "sample": f"oracle on the {ms.nx}x{ms.ny}x{ms.nz}-element grid with the full geomodel: "
+                      f"{visits(ms)} node visits in {dt:.1f}s; full grid projected at {full:.0f}s"}
 
 
 def make_batch(seed: int = 20261204, n: int = 64):
@@ -403,7 +492,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--threads", type=int, default=8, help="models in flight for the batched workload")
     args = ap.parse_args()
-    if args.config == BATCH:
+    if args.config == MAP:
+        if args.impl == "reference":
+            m, gm, cfg = make_map_config()
+            cb = map_cpu_baseline(m, gm, 2 * math.pi * 1e-3)
+            print(json.dumps({"metric": MAP_METRIC, "impl": "reference", "value": cb["value"], "unit": "nodes/s",
+                              "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                              "higher_is_better": True, "dtype": "f64", "config": cfg, "cpu_baseline": cb,
+                              "e2e": {"value": cb["value"], "unit": "nodes/s", "h2d_bytes_per_step": 0,
+                                      "d2h_bytes_per_step": 0}}))
+        else:
+            run_map(args)
+    elif args.config == BATCH:
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no CPU arm; the reference "
                                                                   "solves one model per run"}))

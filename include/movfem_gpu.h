@@ -90,7 +90,7 @@ typedef struct mvf_ctx mvf_ctx;
  * device < 0 keeps the current device. */
 int mvf_create(mvf_ctx **ctx, const mvf_mesh *mesh, int32_t device);
 void mvf_destroy(mvf_ctx *ctx);
-const char *mvf_last_error(const mvf_ctx *ctx);
+const char *mvf_last_error(const mvf_ctx *ctx); /* NULL: this thread's last context-free call */
 
 /* Sizes: free DOFs nne (global_assembly.f90:194), nnz of the full pattern, nnz of its
  * lower triangle (the reference's nnze minus its never-written upper slots). */
@@ -215,6 +215,42 @@ int mvf_spmv_noalloc(mvf_ctx *ctx, int32_t f, const double *x_dev, double *y_dev
  * copied to the device; the refinement loop then starts from b - A x0 instead of b.
  * x0 = NULL drops the guess.  A guess stored for another frequency count is ignored. */
 int mvf_set_guess(mvf_ctx *ctx, const double *x0);
+
+/* ---- Model mapping (the step before the hot path) ----------------------------------
+ * The inner geomodel as read_innermodel / read_geomodel (read_input.f90:104-200) hold
+ * it: mx*my*mz model points, point id p = (im*my + jm)*mz + km (0-based form of the
+ * reference's (im-1)*my*mz+(jm-1)*mz+km), x from xm[im], y from ym[jm], z from zm[p].
+ * Component arrays keep the Fortran layout: ijsigma(isigma,2) is
+ * {i_1..i_isigma, j_1..j_isigma} (1-based tensor indices, i <= j), and sigma(isigma,n)
+ * is [n][isigma] in memory; the same for mu.  isigma = 1: isotropic; imu = 0: mu = mu0
+ * everywhere, 1: isotropic relative mu; more: relative tensor components. */
+typedef struct mvf_model {
+    int32_t mx, my, mz;       /* in_mx, in_my, in_mz */
+    const double *xm;         /* [mx] */
+    const double *ym;         /* [my] */
+    const double *zm;         /* [mx*my*mz] */
+    int32_t isigma;           /* in_isigma (>= 1) */
+    const int32_t *ijsigma;   /* [2*isigma] */
+    const double *sigma;      /* [mx*my*mz][isigma], S/m */
+    int32_t imu;              /* in_imu (>= 0) */
+    const int32_t *ijmu;      /* [2*imu] (unused when imu <= 1) */
+    const double *mu;         /* [mx*my*mz][imu] relative permeability (unused when imu = 0) */
+} mvf_model;
+
+/* Nodal conductivity and permeability of the grid from the inner geomodel
+ * (innermodel_gqg, min_dd_inner, assign_model: geometry.f90:804-1085), which grid_3d
+ * (geometry.f90:106) calls once before the frequency loop.  Reads the grid fields of
+ * `grid` (nodes_per_elem, nx, ny, nz, xp, yp, zp, nextd >= 1, nzl_top + nzl_air >= 1,
+ * quirks; its sigma and mu are ignored).  Each node of the inner elements takes the
+ * first model point (in point order) within 1e-5 m, else the first nearest one; the
+ * extension planes, the bottom layers and the air follow the reference's copy order,
+ * and negative entries then take the value of the node below.  omega: the angular
+ * frequency of the grid time (2*pi*f_1); eps*omega is rounded to FP32 when quirks
+ * carry MVF_Q_FP32_CONST.  sigma_out [npt][6] complex, mu_out [npt][6] (g_sigma,
+ * g_mu).  seconds (optional): device time of the kernels.  Context-free: on error,
+ * mvf_last_error(NULL) gives this thread's message.  device < 0 keeps the current one. */
+int mvf_map_model(const mvf_mesh *grid, const mvf_model *model, double omega, double *sigma_out, double *mu_out,
+                  double *seconds, int32_t device);
 
 /* ---- Learned warm start (no counterpart in the reference) -------------------------
  * A dilated 3-D convolutional operator on a cell grid: nconv 3x3x3 convolutions of

@@ -58,7 +58,7 @@ EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numb
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
            "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many", "mvf_profile_patch",
-           "mvf_set_solver", "mvf_patch_arithmetic"]
+           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
                "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params", "mvf_patch_arithmetic")
 SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
@@ -127,6 +127,7 @@ def load(build: bool = True):
     L.mvf_net_train_step.argtypes = [P, I32, I32, I32, P, P, ctypes.c_float, P]
     L.mvf_spmm_tuning.argtypes = [P]
     L.mvf_spmm_tuning.restype = ctypes.c_char_p
+    L.mvf_map_model.argtypes = [P, P, D, P, P, P, I32]
     for n in EXPORTS:
         if n not in _NOT_STATUS:
             getattr(L, n).restype = ctypes.c_int
@@ -136,6 +137,41 @@ def load(build: bool = True):
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+class _Model(ctypes.Structure):
+    _fields_ = [
+        ("mx", ctypes.c_int32), ("my", ctypes.c_int32), ("mz", ctypes.c_int32), ("xm", ctypes.c_void_p),
+        ("ym", ctypes.c_void_p), ("zm", ctypes.c_void_p), ("isigma", ctypes.c_int32), ("ijsigma", ctypes.c_void_p),
+        ("sigma", ctypes.c_void_p), ("imu", ctypes.c_int32), ("ijmu", ctypes.c_void_p), ("mu", ctypes.c_void_p),
+    ]
+
+
+def map_model(mesh, model, omega: float, device: int = -1, timed: bool = False):
+    """Nodal conductivity and permeability of ``mesh``'s grid from the inner geomodel
+    ``model`` (:class:`movfem_gb300.mesh.GeoModel`) on the GPU (``mvf_map_model``,
+    replacing innermodel_gqg / min_dd_inner / assign_model, geometry.f90:804-1085,
+    which grid_3d calls at geometry.f90:106).  ``omega`` is the grid-time angular
+    frequency 2*pi*f_1.  Returns sigma [npt, 6] complex128 and mu [npt, 6] (plus the
+    kernels' device seconds when ``timed``)."""
+    L = load()
+    xp = np.ascontiguousarray(mesh.xp, dtype=np.float64)
+    yp = np.ascontiguousarray(mesh.yp, dtype=np.float64)
+    zp = np.ascontiguousarray(mesh.zp, dtype=np.float64)
+    g = _Mesh(mesh.nodes_per_elem, mesh.nx, mesh.ny, mesh.nz, _p(xp), _p(yp), _p(zp), None, None,
+              mesh.dirichlet, mesh.inimod, mesh.gpml_sch, mesh.a0, mesh.b0, mesh.nn, mesh.nextd, mesh.nzl_top,
+              mesh.nzl_air, mesh.ztop, mesh.quirks, mesh.h_sigma, 0, None, None)
+    a = model.c_arrays()
+    md = _Model(a["mx"], a["my"], a["mz"], _p(a["xm"]), _p(a["ym"]), _p(a["zm"]), a["isigma"], _p(a["ijsigma"]),
+                _p(a["sigma"]), a["imu"], _p(a["ijmu"]), _p(a["mu"]))
+    sigma = np.empty((mesh.npt, 6), dtype=np.complex128)
+    mu = np.empty((mesh.npt, 6))
+    sec = ctypes.c_double(0.0)
+    rc = L.mvf_map_model(ctypes.byref(g), ctypes.byref(md), float(omega), _p(sigma), _p(mu), ctypes.byref(sec),
+                         device)
+    if rc != 0:
+        raise MVFError(rc, L.mvf_last_error(None).decode())
+    return (sigma, mu, sec.value) if timed else (sigma, mu)
 
 
 def solve_many(problems, tol: float = 1e-10, mode: int = 0, max_iters: int = 5000, nthreads: int = 8):

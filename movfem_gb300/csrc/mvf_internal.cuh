@@ -167,6 +167,9 @@ int assemble_set(Ctx *c, MatrixSet &S, bool gpml, int fset);
 int assemble_rhs(Ctx *c);
 void free_sets(Ctx *c);
 
+// message of this thread's last context-free call (mvf_map_model, mvf_model.cu)
+const char *map_last_error();
+
 // vertex-patch Schwarz preconditioner (mvf_patch.cu)
 int patch_setup(Ctx *c);
 int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **inv_out);

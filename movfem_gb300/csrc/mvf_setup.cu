@@ -524,7 +524,7 @@ extern "C" void mvf_destroy(mvf_ctx *x) {
     delete x;
 }
 
-extern "C" const char *mvf_last_error(const mvf_ctx *x) { return x ? x->c.err.c_str() : "null context"; }
+extern "C" const char *mvf_last_error(const mvf_ctx *x) { return x ? x->c.err.c_str() : map_last_error(); }
 
 extern "C" int mvf_sizes(const mvf_ctx *x, int32_t *nne, int64_t *nnz_full, int64_t *nnz_lower, int32_t *me,
                          int64_t *ne) {

@@ -110,6 +110,115 @@ class Mesh:
         return s.reshape(self.npt, 6)
 
 
+@dataclasses.dataclass
+class GeoModel:
+    """Inner geomodel in the layout read_innermodel / read_geomodel leave it
+    (read_input.f90:104-200): model point p = (im*my + jm)*mz + km at
+    (xm[im], ym[jm], zm[p]) in the grid's coordinates; ``sigma[p, c]`` is component c,
+    whose tensor index is ``ijsigma[c] = (i, j)`` (1-based, "SIGMAij"); ``mu`` likewise
+    (relative permeability), or None for mu = mu0 (in_imu = 0)."""
+    xm: np.ndarray          # [mx]
+    ym: np.ndarray          # [my]
+    zm: np.ndarray          # [mx, my, mz]
+    sigma: np.ndarray       # [mx*my*mz, isigma]
+    ijsigma: np.ndarray     # [isigma, 2]
+    mu: np.ndarray | None = None    # [mx*my*mz, imu]
+    ijmu: np.ndarray | None = None  # [imu, 2]
+
+    @property
+    def shape(self):
+        return self.zm.shape
+
+    def c_arrays(self) -> dict:
+        """Contiguous arrays for the C-ABI: ij tables in the Fortran layout
+        {i_1..i_n, j_1..j_n}."""
+        mx, my, mz = self.zm.shape
+        sig = np.ascontiguousarray(self.sigma, dtype=np.float64).reshape(mx * my * mz, -1)
+        ijs = np.ascontiguousarray(np.asarray(self.ijsigma, dtype=np.int32).reshape(-1, 2).T).reshape(-1)
+        if self.mu is None:
+            mu, ijm, imu = None, None, 0
+        else:
+            mu = np.ascontiguousarray(self.mu, dtype=np.float64).reshape(mx * my * mz, -1)
+            imu = mu.shape[1]
+            ijm = np.ascontiguousarray(np.asarray(self.ijmu, dtype=np.int32).reshape(-1, 2).T).reshape(-1)
+        return dict(mx=mx, my=my, mz=mz, xm=np.ascontiguousarray(self.xm, dtype=np.float64),
+                    ym=np.ascontiguousarray(self.ym, dtype=np.float64),
+                    zm=np.ascontiguousarray(self.zm, dtype=np.float64).reshape(-1), isigma=sig.shape[1],
+                    ijsigma=ijs, sigma=sig, imu=imu, ijmu=ijm, mu=mu)
+
+
+FULL_TENSOR = np.array([[1, 1], [1, 2], [1, 3], [2, 2], [2, 3], [3, 3]], dtype=np.int32)
+
+
+def synthetic_geomodel(seed: int, mesh: "Mesh", *, spacing: float, depth: float, anisotropic: bool = False,
+                       relief: float = 0.0, mu_tensor: bool = False, on_nodes: bool = False,
+                       node_stride: int = 1, topo_fn=None) -> GeoModel:
+    """A seeded inner geomodel over ``mesh``'s core: model points every ``spacing`` m in
+    x and y over the inner elements and down to ``depth`` below the surface, z per
+    column shifted by up to ``relief`` m; layered conductivity (log-uniform
+    [1e-3, 1] S/m) with two blocks (log-uniform [1e-3, 10] S/m).  ``anisotropic``
+    gives each point a full SPD tensor R diag(l) R^T (six components, off-diagonals of
+    either sign); ``mu_tensor`` adds relative permeabilities near 1 as six components;
+    ``on_nodes`` puts the points on every ``node_stride``-th grid node of the inner
+    columns instead (exact hits, distance 0).  ``topo_fn(x, y)`` (the grid's surface
+    relief) shifts each model column with the surface."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    o = mesh.nord - 1
+    E = mesh.nextd * o
+    x0, x1 = mesh.xp[E], mesh.xp[mesh.nnx - 1 - E]
+    y0, y1 = mesh.yp[E], mesh.yp[mesh.nny - 1 - E]
+    zs = mesh.ztop
+    if on_nodes:
+        # every node_stride-th grid node of the inner columns, from the bottom to the surface
+        ksurf = mesh.nnz - (mesh.nzl_top + mesh.nzl_air) * o - 1
+        ii = np.arange(E, mesh.nnx - E, node_stride)
+        jj = np.arange(E, mesh.nny - E, node_stride)
+        kk = np.arange(0, ksurf + 1, node_stride)
+        xm, ym = mesh.xp[ii].copy(), mesh.yp[jj].copy()
+        zm = mesh.zp.reshape(mesh.nnx, mesh.nny, mesh.nnz)[np.ix_(ii, jj, kk)].copy()
+    else:
+        xm = np.arange(x0 + 0.5 * spacing, x1, spacing)
+        ym = np.arange(y0 + 0.5 * spacing, y1, spacing)
+        nzm = max(2, int(depth // spacing))
+        zline = zs - spacing * (0.5 + np.arange(nzm))[::-1]
+        shift = relief * rng.uniform(-1, 1, (xm.size, ym.size, 1))
+        zm = np.broadcast_to(zline[None, None, :] + shift, (xm.size, ym.size, nzm)).copy()
+    mx, my, mz = zm.shape
+    X, Y = np.meshgrid(xm, ym, indexing="ij")
+    hs = np.zeros((mx, my, 1))
+    if topo_fn is not None and not on_nodes:
+        hs = topo_fn(X, Y)[..., None]
+        zm = zm + hs
+    X = np.broadcast_to(X[..., None], zm.shape)
+    Y = np.broadcast_to(Y[..., None], zm.shape)
+    d = (zs + hs) - zm
+    lsig = 10.0 ** rng.uniform(-3, 0, 3)
+    iface = np.sort(rng.uniform(0.1, 0.9, 2)) * max(depth, 1.0)
+    s = lsig[np.searchsorted(iface, d)]
+    for _ in range(2):
+        c = rng.uniform([x0, y0, 0.0], [x1, y1, max(depth, 1.0)])
+        h = rng.uniform(0.1, 0.3, 3) * np.array([x1 - x0, y1 - y0, max(depth, 1.0)])
+        inside = (np.abs(X - c[0]) <= h[0]) & (np.abs(Y - c[1]) <= h[1]) & (np.abs(d - c[2]) <= h[2])
+        s = np.where(inside, 10.0 ** rng.uniform(-3, 1), s)
+    n = mx * my * mz
+    if anisotropic:
+        q, _ = np.linalg.qr(rng.normal(size=(n, 3, 3)))
+        lam = s.reshape(n, 1) * 10.0 ** rng.uniform(-1, 1, (n, 3))
+        T = np.einsum("nij,nj,nkj->nik", q, lam, q)
+        sigma = np.stack([T[:, i - 1, j - 1] for i, j in FULL_TENSOR], axis=1)
+        ijs = FULL_TENSOR.copy()
+    else:
+        sigma = s.reshape(n, 1).copy()
+        ijs = np.array([[1, 1]], dtype=np.int32)
+    mu = ijm = None
+    if mu_tensor:
+        mu = np.zeros((n, 6))
+        mu[:, [0, 3, 5]] = 1.0 + rng.uniform(0, 0.5, (n, 3))
+        mu[:, [1, 2, 4]] = rng.uniform(-0.05, 0.05, (n, 3))
+        ijm = FULL_TENSOR.copy()
+    return GeoModel(xm=xm, ym=ym, zm=zm, sigma=sigma, ijsigma=ijs, mu=mu, ijmu=ijm)
+
+
 def _padding(n: int, d: float) -> np.ndarray:
     return np.array([GROWTH * i * d for i in range(1, n + 1)])
 

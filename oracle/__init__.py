@@ -35,7 +35,7 @@ def build(force: bool = False) -> str:
     os.makedirs(_BUILD, exist_ok=True)
     if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
         tmp = _LIB + f".{os.getpid()}.tmp"
-        subprocess.check_call(["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-std=c99", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
         os.replace(tmp, _LIB)
     return _LIB
 
@@ -75,12 +75,44 @@ def lib():
             L.orc_node_fields.argtypes = [P, P, I32, D, P, P, P, P, P, P]
             L.orc_check_sharing.restype = D
             L.orc_check_sharing.argtypes = [P]
+            L.orc_map_model.restype = ctypes.c_int
+            L.orc_map_model.argtypes = [P, P, D, P, P]
             _lib = L
     return _lib
 
 
 def _ptr(a):
     return a.ctypes.data if a is not None else None
+
+
+class _Model(ctypes.Structure):
+    _fields_ = [
+        ("mx", ctypes.c_int32), ("my", ctypes.c_int32), ("mz", ctypes.c_int32), ("xm", ctypes.c_void_p),
+        ("ym", ctypes.c_void_p), ("zm", ctypes.c_void_p), ("isigma", ctypes.c_int32), ("ijsigma", ctypes.c_void_p),
+        ("sigma", ctypes.c_void_p), ("imu", ctypes.c_int32), ("ijmu", ctypes.c_void_p), ("mu", ctypes.c_void_p),
+    ]
+
+
+def map_model(mesh, model, omega):
+    """Nodal sigma [npt, 6] complex and mu [npt, 6] of ``mesh``'s grid from the inner
+    geomodel ``model`` (a ``movfem_gb300.mesh.GeoModel``), restating innermodel_gqg /
+    min_dd_inner / assign_model (geometry.f90:804-1085) sequentially."""
+    a = model.c_arrays()
+    dummy = np.zeros(1)
+    o = Oracle.__new__(Oracle)
+    o.mesh, o.quirks = mesh, mesh.quirks
+    o.xp = np.ascontiguousarray(mesh.xp, dtype=np.float64)
+    o.yp = np.ascontiguousarray(mesh.yp, dtype=np.float64)
+    o.zp = np.ascontiguousarray(mesh.zp, dtype=np.float64)
+    o.sigma, o.mu, o.l_sigma, o.l_dz = dummy, dummy, None, None
+    md = _Model(a["mx"], a["my"], a["mz"], _ptr(a["xm"]), _ptr(a["ym"]), _ptr(a["zm"]), a["isigma"],
+                _ptr(a["ijsigma"]), _ptr(a["sigma"]), a["imu"], _ptr(a["ijmu"]), _ptr(a["mu"]))
+    sigma = np.empty((mesh.npt, 6), dtype=np.complex128)
+    mu = np.empty((mesh.npt, 6))
+    rc = lib().orc_map_model(o._s(), ctypes.byref(md), float(omega), _ptr(sigma), _ptr(mu))
+    if rc != 0:
+        raise RuntimeError(f"oracle model mapping failed rc={rc}")
+    return sigma, mu
 
 
 class Oracle:

@@ -1223,3 +1223,165 @@ double orc_check_sharing(const orc_mesh *m) {
             }
     return worst;
 }
+
+/* ------------------------------------------------------------------ model mapping */
+/* Tensor slot of a model component (assign_model's select case, geometry.f90:1053-1080):
+ * (1, j) -> j, (2 or 3, j) -> i + j, 1-based packed (xx, xy, xz, yy, yz, zz). */
+static int map_slot(int i, int j) { return i == 1 ? j : i + j; }
+
+static int map_components_ok(int32_t n, const int32_t *ij) {
+    int32_t c;
+    for (c = 0; c < n; c++)
+        if (ij[c] < 1 || ij[c] > 3 || ij[n + c] < 1 || ij[n + c] > 3) return 0;
+    return 1;
+}
+
+/* assign_model (geometry.f90:1037-1085): node id takes point p unless already valued.
+ * cmplx(0.d0, eps*omega) has the default kind, so ieps arrives FP32-rounded (Q4). */
+static void map_assign(const orc_model *md, int64_t p, double ieps, unsigned char *valued, int64_t id,
+                       double *sigma, double *mu) {
+    const double mu0 = 4.0 * PI * 1.e-7;
+    double *s = sigma + id * 12, *u = mu + id * 6;
+    int c;
+    if (valued[id]) return;
+    for (c = 0; c < 12; c++) s[c] = 0.0;
+    if (md->isigma == 1) {
+        const double v = md->sigma[p];
+        s[0] = v; s[1] = ieps;   /* sigma(1) + cmplx(0, eps*omega) */
+        s[6] = v; s[7] = ieps;
+        s[10] = v; s[11] = ieps;
+    } else {
+        for (c = 0; c < md->isigma; c++) {
+            const int slot = map_slot(md->ijsigma[c], md->ijsigma[md->isigma + c]) - 1;
+            s[2 * slot] = md->sigma[p * md->isigma + c];
+            s[2 * slot + 1] = 0.0;
+        }
+        s[0] = s[0] + 0.0; s[1] = s[1] + ieps;
+        s[6] = s[6] + 0.0; s[7] = s[7] + ieps;
+        s[10] = s[10] + 0.0; s[11] = s[11] + ieps;
+    }
+    for (c = 0; c < 6; c++) u[c] = 0.0;
+    if (md->imu <= 1) {
+        /* imu = 0: read_geomodel fills in_mu(1,:) with 1 (read_input.f90:188-190) */
+        const double v = mu0 * (md->imu == 0 ? 1.0 : md->mu[p]);
+        u[0] = v; u[3] = v; u[5] = v;
+    } else {
+        for (c = 0; c < md->imu; c++)
+            u[map_slot(md->ijmu[c], md->ijmu[md->imu + c]) - 1] = mu0 * md->mu[p * md->imu + c];
+    }
+    valued[id] = 1;
+}
+
+/* min_dd_inner's scan for one node (geometry.f90:971-1031): model points in order,
+ * the first within 1e-5 wins (assign_model marks the node valued at once), else the
+ * first with the smallest distance.  Returns the point, or -1 if none is below 1e20. */
+static int64_t map_search(const orc_model *md, double x, double y, double z) {
+    double ddmin = 1.e20;
+    int64_t best = -1;
+    int32_t im, jm, km;
+    for (im = 0; im < md->mx; im++)
+        for (jm = 0; jm < md->my; jm++)
+            for (km = 0; km < md->mz; km++) {
+                const int64_t p = ((int64_t)im * md->my + jm) * md->mz + km;
+                const double dx = x - md->xm[im], dy = y - md->ym[jm], dz = z - md->zm[p];
+                const double dd = sqrt(dx * dx + dy * dy + dz * dz);
+                if (dd <= 1.e-5) return p;
+                if (dd < ddmin) { ddmin = dd; best = p; }
+            }
+    return best;
+}
+
+static void map_copy(double *sigma, double *mu, unsigned char *valued, int64_t id, int64_t ip) {
+    if (valued[id]) return;
+    memcpy(sigma + id * 12, sigma + ip * 12, 12 * sizeof(double));
+    memcpy(mu + id * 6, mu + ip * 6, 6 * sizeof(double));
+    valued[id] = 1;
+}
+
+int orc_map_model(const orc_mesh *m, const orc_model *md, double omega, double *sigma, double *mu) {
+    int32_t nnx, nny, nnz;
+    int64_t npt, id, nyz;
+    const int o = m->nodes_per_elem == 8 ? 1 : 2, nord = o + 1;
+    const int nair = m->nzl_top + m->nzl_air, E = m->nextd * o;
+    const double ieps = r32(m, EPS0 * omega), mu0 = 4.0 * PI * 1.e-7;
+    int ie, je, ke, ii, jj, kk, c;
+    int64_t im, jm, km;
+    unsigned char *valued;
+    if (m->nextd < 1 || nair < 1 || m->nx - 2 * m->nextd < 1 || m->ny - 2 * m->nextd < 1 ||
+        m->nz - nair < m->nextd)
+        return -1;
+    if (md->mx < 1 || md->my < 1 || md->mz < 1 || md->isigma < 1 || md->imu < 0) return -1;
+    if (md->isigma > 1 && !map_components_ok(md->isigma, md->ijsigma)) return -1;
+    if (md->imu > 1 && !map_components_ok(md->imu, md->ijmu)) return -1;
+    orc_num_nodes(m, &nnx, &nny, &nnz, &npt);
+    nyz = (int64_t)nny * nnz;
+    valued = (unsigned char *)calloc((size_t)npt, 1);
+    if (!valued) return -1;
+    for (id = 0; id < npt; id++) {  /* g_sigma = cmplx(-1,0); g_mu = -1 */
+        for (c = 0; c < 6; c++) {
+            sigma[id * 12 + 2 * c] = -1.0;
+            sigma[id * 12 + 2 * c + 1] = 0.0;
+            mu[id * 6 + c] = -1.0;
+        }
+    }
+    /* element loop (geometry.f90:832-852); 1-based element indices as the reference */
+    for (ie = m->nextd + 1; ie <= m->nx - m->nextd; ie++)
+        for (je = m->nextd + 1; je <= m->ny - m->nextd; je++)
+            for (ke = m->nextd; ke <= m->nz - nair; ke++) {
+                const int64_t no = (int64_t)(ie - 1) * o * nyz + (int64_t)(je - 1) * o * nnz + (int64_t)(ke - 1) * o;
+                for (ii = 0; ii < nord; ii++)
+                    for (jj = 0; jj < nord; jj++)
+                        for (kk = 0; kk < nord; kk++) {
+                            const int64_t nid = no + ii * nyz + (int64_t)jj * nnz + kk;
+                            const int64_t p = map_search(md, m->xp[(ie - 1) * o + ii], m->yp[(je - 1) * o + jj],
+                                                         m->zp[nid]);
+                            if (p < 0) { free(valued); return -2; }
+                            map_assign(md, p, ieps, valued, nid, sigma, mu);
+                        }
+            }
+    /* 1. (y,z) planes (geometry.f90:854-883); k range 1-based [E, nnz - nair*o] */
+    for (im = 0; im < E; im++)
+        for (jm = E; jm < nny - E; jm++)
+            for (km = E - 1; km < nnz - (int64_t)nair * o; km++)
+                map_copy(sigma, mu, valued, im * nyz + jm * nnz + km, (int64_t)E * nyz + jm * nnz + km);
+    for (im = nnx - E; im < nnx; im++)
+        for (jm = E; jm < nny - E; jm++)
+            for (km = E - 1; km < nnz - (int64_t)nair * o; km++)
+                map_copy(sigma, mu, valued, im * nyz + jm * nnz + km, (int64_t)(nnx - E - 1) * nyz + jm * nnz + km);
+    /* 2. (x,z) planes (geometry.f90:885-913) */
+    for (im = 0; im < nnx; im++)
+        for (jm = 0; jm < E; jm++)
+            for (km = E - 1; km < nnz - (int64_t)nair * o; km++)
+                map_copy(sigma, mu, valued, im * nyz + jm * nnz + km, im * nyz + (int64_t)E * nnz + km);
+    for (im = 0; im < nnx; im++)
+        for (jm = nny - E; jm < nny; jm++)
+            for (km = E - 1; km < nnz - (int64_t)nair * o; km++)
+                map_copy(sigma, mu, valued, im * nyz + jm * nnz + km, im * nyz + (int64_t)(nny - E - 1) * nnz + km);
+    /* 3. (x,y) planes below the inner elements (geometry.f90:915-926) */
+    for (im = 0; im < nnx; im++)
+        for (jm = 0; jm < nny; jm++)
+            for (km = 0; km < E - 1; km++)
+                map_copy(sigma, mu, valued, im * nyz + jm * nnz + km, im * nyz + jm * nnz + (E - 1));
+    /* 4. air (geometry.f90:928-940) */
+    for (im = 0; im < nnx; im++)
+        for (jm = 0; jm < nny; jm++)
+            for (km = nnz - (int64_t)nair * o; km < nnz; km++) {
+                id = im * nyz + jm * nnz + km;
+                for (c = 0; c < 12; c++) sigma[id * 12 + c] = 0.0;
+                for (c = 0; c < 6; c++) mu[id * 6 + c] = 0.0;
+                sigma[id * 12 + 1] = ieps; sigma[id * 12 + 7] = ieps; sigma[id * 12 + 11] = ieps;
+                mu[id * 6 + 0] = mu0; mu[id * 6 + 3] = mu0; mu[id * 6 + 5] = mu0;
+            }
+    /* 5. negative entries take the node below (geometry.f90:942-955).  The reference's
+     * first node would read before the start of its arrays; it is left as it is. */
+    for (id = 1; id < npt; id++)
+        for (c = 0; c < 6; c++) {
+            if (sigma[id * 12 + 2 * c] < 0) {
+                sigma[id * 12 + 2 * c] = sigma[(id - 1) * 12 + 2 * c];
+                sigma[id * 12 + 2 * c + 1] = sigma[(id - 1) * 12 + 2 * c + 1];
+            }
+            if (mu[id * 6 + c] < 0) mu[id * 6 + c] = mu[(id - 1) * 6 + c];
+        }
+    free(valued);
+    return 0;
+}

@@ -99,6 +99,30 @@ int orc_receivers(const orc_mesh *m, const int32_t *gne, int32_t nne, double ome
 int orc_node_fields(const orc_mesh *m, const int32_t *gne, int32_t nne, double omega, const double *x,
                     double *E, double *H, double *Z, double *rho, double *phi);
 
+/* Inner geomodel (read_input.f90:104-200): point id p = (im*my + jm)*mz + km;
+ * ijsigma/ijmu in the Fortran layout {i_1..i_n, j_1..j_n}; sigma [npts][isigma],
+ * mu [npts][imu] (relative). */
+typedef struct orc_model {
+    int32_t mx, my, mz;
+    const double *xm, *ym, *zm;
+    int32_t isigma;
+    const int32_t *ijsigma;
+    const double *sigma;
+    int32_t imu;
+    const int32_t *ijmu;
+    const double *mu;
+} orc_model;
+
+/* Nodal sigma [npt][6] complex and mu [npt][6] of the grid from the inner geomodel,
+ * in the reference's sequence (innermodel_gqg, min_dd_inner, assign_model:
+ * geometry.f90:804-1085): brute-force search of every model point for each node of
+ * each inner element (element order ie, je, ke; first point within 1e-5 m, else first
+ * nearest), copies to the extension planes, bottom layers, air, then negative entries
+ * from the node below.  The grid fields of m are read (sigma/mu ignored).  Returns 0,
+ * -1 on a size error, -2 when a node finds no model point (the reference would index
+ * sigma(:,-1)). */
+int orc_map_model(const orc_mesh *m, const orc_model *md, double omega, double *sigma, double *mu);
+
 /* Basis self-check of the reference's vf_check_sharing kind: maximum mismatch of the
  * tangential component of shared edge basis functions between face neighbours. */
 double orc_check_sharing(const orc_mesh *m);

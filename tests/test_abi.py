@@ -49,3 +49,25 @@ def test_mesh_struct_layout_matches_the_header():
         out = [int(v) for v in subprocess.check_output([exe]).split()]
     assert out[0] == ctypes.sizeof(api._Mesh)
     assert out[1:] == [getattr(api._Mesh, f).offset for f in fields]
+
+
+def test_model_struct_layout_matches_the_header():
+    """The ctypes mirrors of mvf_model (library and oracle) have the C struct's size and
+    field offsets."""
+    import subprocess
+    import tempfile
+
+    import oracle
+    fields = [f for f, _ in api._Model._fields_]
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.c")
+        body = "".join(f'printf("%zu\\n", offsetof(mvf_model, {f}));' for f in fields)
+        open(src, "w").write('#include <stddef.h>\n#include <stdio.h>\n#include "movfem_gpu.h"\n'
+                             'int main(void){printf("%zu\\n", sizeof(mvf_model));' + body + 'return 0;}\n')
+        exe = os.path.join(d, "t")
+        subprocess.check_call(["gcc", "-std=c99", "-I", HDR, src, "-o", exe])
+        out = [int(v) for v in subprocess.check_output([exe]).split()]
+    for S in (api._Model, oracle._Model):
+        assert [f for f, _ in S._fields_] == fields
+        assert out[0] == ctypes.sizeof(S)
+        assert out[1:] == [getattr(S, f).offset for f in fields]
