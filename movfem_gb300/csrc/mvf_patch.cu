@@ -244,22 +244,26 @@ __global__ void __launch_bounds__(128) patch_apply_kernel(int64_t p0, int64_t p1
 // GB300 runs FP64 at a small fraction of its FP32 rate, and the FP64 application above
 // is bound by the FP64 pipe.  Here every inverse entry is held as an unevaluated sum
 // hi + lo of two FP32 numbers (same 16 bytes per complex entry), the right-hand sides
-// likewise, and the products and sums run in float-float arithmetic on the FP32 pipe
-// (Dekker/Knuth error-free transformations: a product's rounding error by FMA, a
-// sum's by TwoSum), about 44 significant bits, against 24 for plain FP32 -- enough for
-// inverses whose air-gradient components dwarf the rest.
+// likewise, and the products and sums run on the FP32 pipe with error-free
+// transformations (Dekker/Knuth: a product's rounding error by FMA, a sum's by TwoSum),
+// accumulated as a compensated dot product: about as accurate as a sum in twice FP32's
+// precision, against 24 bits for plain FP32 -- enough for inverses whose air-gradient
+// components dwarf the rest.
 
-// s (hi, lo) += a * b, each operand split hi + lo
-__device__ __forceinline__ void ff_mac(float &sh, float &sl, float ah, float al, float bh, float bl) {
+// s += a*b with a, b float-float, as a compensated dot product (Ogita, Rump and Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005, Dot2): the high part
+// by TwoSum, every rounding error (the product's by FMA, the cross terms, the sum's)
+// collected in a plain FP32 low part without renormalising at each step.  The high
+// part's dependency chain is one addition per product.
+__device__ __forceinline__ void dot2_mac(float &sh, float &sl, float ah, float al, float bh, float bl) {
     const float p = ah * bh;
     float e = fmaf(ah, bh, -p);
     e = fmaf(ah, bl, fmaf(al, bh, e));
     const float t = sh + p;
     const float bb = t - sh;
     const float err = (sh - (t - bb)) + (p - bb);
-    const float lo = sl + e + err;
-    sh = t + lo;
-    sl = lo - (sh - t);
+    sh = t;
+    sl += e + err;
 }
 
 // The inverses span many orders of magnitude (air patches, PML stretch), beyond what
@@ -354,10 +358,10 @@ __global__ void __launch_bounds__(128) patch_apply_ff_kernel(int64_t p0, int64_t
                 const float4 a = Ai[j];
                 const float4 x = rsf[j * R + q];
                 // (a.re + i a.im)(x.re + i x.im)
-                ff_mac(rh, rl, a.x, a.z, x.x, x.z);
-                ff_mac(rh, rl, -a.y, -a.w, x.y, x.w);
-                ff_mac(ih, il, a.x, a.z, x.y, x.w);
-                ff_mac(ih, il, a.y, a.w, x.x, x.z);
+                dot2_mac(rh, rl, a.x, a.z, x.x, x.z);
+                dot2_mac(rh, rl, -a.y, -a.w, x.y, x.w);
+                dot2_mac(ih, il, a.x, a.z, x.y, x.w);
+                dot2_mac(ih, il, a.y, a.w, x.x, x.z);
             }
             const double d = scale[(int64_t)min(q / npol, nfi - 1) * ndof + b0 + i];
             TV &o = z[(int64_t)pdof[b0 + i] * R + q];
