@@ -67,6 +67,9 @@ def python_map(m, gm, omega):
         if gm.mu is None:
             for c in (0, 3, 5):
                 u[c] = MU0 * 1.0
+        elif gm.mu.reshape(mx * my * mz, -1).shape[1] == 1:
+            for c in (0, 3, 5):
+                u[c] = MU0 * gm.mu.reshape(-1)[p - 1]
         else:
             mu_in = gm.mu.reshape(mx * my * mz, -1)
             ijm = np.asarray(gm.ijmu).reshape(-1, 2)
@@ -155,16 +158,26 @@ CASES = [
     (20, 2, 0.0, dict(spacing=85.0, depth=350.0, anisotropic=True, mu_tensor=True)),
     (27, 2, 40.0, dict(spacing=60.0, depth=300.0, relief=10.0)),
     (20, 2, 0.0, dict(spacing=0.0, depth=0.0, on_nodes=True, node_stride=2)),
+    (8, 2, 20.0, dict(spacing=80.0, depth=300.0, relief=15.0, mu_iso=True)),
 ]
+IDS = ["linear-iso", "linear-aniso-topo-nextd1", "quadratic-aniso-mu-tensor", "lagrangian-iso-topo",
+       "quadratic-points-on-nodes", "linear-iso-mu-topo"]
 
 
 def _model(case, seed=3):
     order, nextd, topo, kw = case
+    kw = dict(kw)
+    mu_iso = kw.pop("mu_iso", False)
     m = small_grid(order, nextd=nextd, topo=topo)
-    return m, M.synthetic_geomodel(seed, m, **kw)
+    gm = M.synthetic_geomodel(seed, m, **kw)
+    if mu_iso:  # in_imu = 1: one isotropic relative permeability per point
+        rng = np.random.Generator(np.random.PCG64(seed))
+        gm.mu = 1.0 + rng.uniform(0.0, 2.0, (gm.zm.size, 1))
+        gm.ijmu = np.array([[1, 1]], dtype=np.int32)
+    return m, gm
 
 
-@pytest.mark.parametrize("case", CASES[:3] + CASES[4:], ids=lambda c: f"order{c[0]}-nextd{c[1]}")
+@pytest.mark.parametrize("case", CASES[:3] + CASES[4:], ids=IDS[:3] + IDS[4:])
 def test_oracle_matches_python_restatement(case):
     m, gm = _model(case)
     w = 2 * math.pi * 0.1
@@ -268,7 +281,7 @@ def test_pruned_scan_picks_the_reference_point():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", CASES, ids=lambda c: f"order{c[0]}-nextd{c[1]}-{'aniso' if c[3].get('anisotropic') else 'iso'}")
+@pytest.mark.parametrize("case", CASES, ids=IDS)
 def test_gpu_map_matches_oracle_bit_exact(case):
     from movfem_gb300 import api
     m, gm = _model(case)
