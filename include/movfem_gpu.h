@@ -248,7 +248,8 @@ typedef struct mvf_model {
  * frequency of the grid time (2*pi*f_1); eps*omega is rounded to FP32 when quirks
  * carry MVF_Q_FP32_CONST.  sigma_out [npt][6] complex, mu_out [npt][6] (g_sigma,
  * g_mu).  seconds (optional): device time of the kernels.  Context-free: on error,
- * mvf_last_error(NULL) gives this thread's message.  device < 0 keeps the current one. */
+ * mvf_last_error(NULL) gives this thread's message.  device < 0 uses the current
+ * device; otherwise that device, and the caller's current device is restored. */
 int mvf_map_model(const mvf_mesh *grid, const mvf_model *model, double omega, double *sigma_out, double *mu_out,
                   double *seconds, int32_t device);
 

@@ -333,8 +333,20 @@ extern "C" int mvf_map_model(const mvf_mesh *grid, const mvf_model *md, double o
     const double ieps = (m.quirks & MVF_Q_FP32_CONST) ? (double)(float)(8.854187817e-12 * omega)
                                                       : 8.854187817e-12 * omega;
 
+    // the caller's current device is restored on return (after the buffers are freed)
+    struct DeviceGuard {
+        int prev = -1;
+        ~DeviceGuard() {
+            if (prev >= 0) cudaSetDevice(prev);
+        }
+    } guard;
     if (device >= 0) {
-        cudaError_t e = cudaSetDevice(device);
+        int cur = 0;
+        cudaError_t e = cudaGetDevice(&cur);
+        if (e == cudaSuccess && cur != device) {
+            e = cudaSetDevice(device);
+            if (e == cudaSuccess) guard.prev = cur;
+        }
         if (e != cudaSuccess) return map_fail(MVF_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     }
     DevBuf bxp, byp, bzp, bxm, bym, bzm, bsig, bmu, bs, bu, bv, berr;
@@ -370,8 +382,12 @@ extern "C" int mvf_map_model(const mvf_mesh *grid, const mvf_model *md, double o
     uint8_t *val = (uint8_t *)bv.p;
 
     cudaEvent_t t0 = nullptr, t1 = nullptr;
-    cudaEventCreate(&t0);
-    cudaEventCreate(&t1);
+    e = cudaEventCreate(&t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&t1);
+    if (e != cudaSuccess) {
+        if (t0) cudaEventDestroy(t0);
+        return map_fail(MVF_E_CUDA, std::string("model mapping events: ") + cudaGetErrorString(e));
+    }
     cudaEventRecord(t0, 0);
     map_init<<<grid_for(npt, 256), 256>>>(npt, sig, mu, val);
     count_launch();
