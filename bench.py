@@ -289,22 +289,9 @@ def make_map_config(small: bool = False):
     +-300 m) and an inner geomodel of one point per core cell (96x96x64 points at the
     cell centres, following the topography) with a full 6-component anisotropic sigma
     and three layers.  ``small`` gives the same kind at 8x8x6 cells (the CPU sample)."""
-    rng = np.random.Generator(np.random.PCG64(20261205))
+    from movfem_gb300.profile_map import grid_and_model
     n, nz = (8, 6) if small else (96, 64)
-    d = 25.0
-    L = n * d
-    g = [(rng.uniform(0, L), rng.uniform(0, L), rng.uniform(-300, 300), rng.uniform(300, 1500)) for _ in range(5)]
-
-    def topo(x, y):
-        h = np.zeros_like(x, dtype=np.float64)
-        for cx, cy, a, w in g:
-            h = h + a * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * w * w))
-        return np.clip(h, -300.0, 300.0)
-
-    m = M.build_mesh(nodes_per_elem=27, ncx=n, ncy=n, ncz_earth=nz, dx=d, dy=d, dz=d, n_air=10, dz_air=2 * d,
-                     nextd=8, sigma_fn=lambda x, y, dep: 0.01 + 0 * x, omega1=2 * math.pi * 1e-3, topo_fn=topo,
-                     dirichlet=0, gpml_sch=1)
-    gm = M.synthetic_geomodel(20261206, m, spacing=d, depth=nz * d, anisotropic=True, relief=0.0, topo_fn=topo)
+    m, gm = grid_and_model(n, nz)
     cfg = {"workload": f"model-map lagrangian-27 {n}x{n}x{nz}+8pad+10air topo+-300m, "
                        f"{gm.zm.shape[0]}x{gm.zm.shape[1]}x{gm.zm.shape[2]} model points, 6-component sigma",
            "npt": int(m.npt), "model_points": int(gm.zm.size)}
