@@ -15,6 +15,11 @@
 //     skipped point's rounded distance is > T: it could be neither within 1e-5 nor a
 //     new minimum.  The points that remain see the reference's comparisons (<= 1e-5
 //     first, strict < for the minimum), so ties resolve to the same point.
+//  3. where xm, ym or a column's zm are sorted (ascending; columns either way), the
+//     rows, columns or points whose own squared term is within T^2 (1 + 1e-14) form one
+//     contiguous run -- the rounded square of a rounded difference is monotone on each
+//     side of the node's coordinate -- found by binary search; everything outside that
+//     run is exactly what step 2 would skip.  Unsorted arrays are scanned in full.
 //
 // Distances are the reference's sqrt((x-xm)^2 + (y-ym)^2 + (z-zm)^2) with explicitly
 // rounded operations (no contraction into FMA), so the comparisons see the same
@@ -48,6 +53,8 @@ struct MapDims {
 struct ModelDev {
     int32_t mx, my, mz, isigma, imu;
     const double *xm, *ym, *zm, *sigma, *mu;
+    const int8_t *zsort;                 // [mx*my]: +1 zm ascending, -1 descending, 0 neither
+    int32_t xsorted, ysorted;            // xm / ym ascending
     int8_t slot_sigma[16], slot_mu[16];  // component -> 0-based packed slot
 };
 
@@ -61,6 +68,45 @@ __device__ __forceinline__ double sq(double a) { return __dmul_rn(a, a); }
 // reference distance: sqrt(((x-xm)^2 + (y-ym)^2) + (z-zm)^2), every step rounded
 __device__ __forceinline__ double part_xy(double x, double y, double xm, double ym) {
     return __dadd_rn(sq(__dsub_rn(x, xm)), sq(__dsub_rn(y, ym)));
+}
+
+// [lo, hi] of the entries v[0..n) (sorted: dir +1 ascending, -1 descending) whose
+// rounded squared difference to t is <= T2; lo > hi when there is none.  The predicate
+// "on t's lower side, or close enough" is monotone along the array, and so is "on t's
+// upper side, or close enough", so two bisections find the run.
+__device__ __forceinline__ int2 close_run(const double *__restrict__ v, int n, int dir, double t, double T2) {
+    int lo = 0, hi = n;  // first c with (past t or close)
+    while (lo < hi) {
+        const int c = (lo + hi) >> 1;
+        const double a = __ldg(v + c);
+        const bool past = dir > 0 ? a >= t : a <= t;
+        if (past || sq(__dsub_rn(t, a)) <= T2) hi = c;
+        else lo = c + 1;
+    }
+    const int first = lo;
+    lo = -1;
+    hi = n - 1;  // last c with (before t or close)
+    while (lo < hi) {
+        const int c = (lo + hi + 1) >> 1;
+        const double a = __ldg(v + c);
+        const bool before = dir > 0 ? a <= t : a >= t;
+        if (before || sq(__dsub_rn(t, a)) <= T2) lo = c;
+        else hi = c - 1;
+    }
+    return make_int2(first, lo);
+}
+
+// index of an entry of the ascending v[0..n) nearest to t (any one of equal distance)
+__device__ __forceinline__ int nearest_sorted(const double *__restrict__ v, int n, double t) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int c = (lo + hi) >> 1;
+        if (__ldg(v + c) < t) lo = c + 1;
+        else hi = c;
+    }
+    if (lo == n) return n - 1;
+    if (lo > 0 && fabs(t - __ldg(v + lo - 1)) < fabs(__ldg(v + lo) - t)) return lo - 1;
+    return lo;
 }
 
 __device__ void assign(const ModelDev &m, int64_t p, double ieps, double *__restrict__ sigma,
@@ -111,20 +157,42 @@ __global__ void __launch_bounds__(256) map_nearest(MapDims g, ModelDev m, double
         const double x = xp[i], y = yp[j], z = zp[id];
         // 1. seed column: nearest xm and nearest ym
         int ia = 0, ja = 0;
-        double bx = fabs(x - __ldg(m.xm)), by = fabs(y - __ldg(m.ym));
-        for (int a = 1; a < m.mx; ++a) {
-            const double v = fabs(x - __ldg(m.xm + a));
-            if (v < bx) { bx = v; ia = a; }
+        if (m.xsorted) {
+            ia = nearest_sorted(m.xm, m.mx, x);
+        } else {
+            double bx = fabs(x - __ldg(m.xm));
+            for (int a = 1; a < m.mx; ++a) {
+                const double v = fabs(x - __ldg(m.xm + a));
+                if (v < bx) { bx = v; ia = a; }
+            }
         }
-        for (int b = 1; b < m.my; ++b) {
-            const double v = fabs(y - __ldg(m.ym + b));
-            if (v < by) { by = v; ja = b; }
+        if (m.ysorted) {
+            ja = nearest_sorted(m.ym, m.my, y);
+        } else {
+            double by = fabs(y - __ldg(m.ym));
+            for (int b = 1; b < m.my; ++b) {
+                const double v = fabs(y - __ldg(m.ym + b));
+                if (v < by) { by = v; ja = b; }
+            }
         }
         double seed = FAR;
         {
             const double cxy = part_xy(x, y, __ldg(m.xm + ia), __ldg(m.ym + ja));
             const double *zc = m.zm + ((int64_t)ia * m.my + ja) * m.mz;
-            for (int c = 0; c < m.mz; ++c) {
+            const int dir = m.zsort[(int64_t)ia * m.my + ja];
+            int c0 = 0, c1 = m.mz - 1;
+            if (dir != 0) {
+                // the entries either side of z in the sorted column
+                int lo = 0, hi = m.mz;
+                while (lo < hi) {
+                    const int c = (lo + hi) >> 1;
+                    if (dir > 0 ? __ldg(zc + c) < z : __ldg(zc + c) > z) lo = c + 1;
+                    else hi = c;
+                }
+                c0 = max(lo - 1, 0);
+                c1 = min(lo, m.mz - 1);
+            }
+            for (int c = c0; c <= c1; ++c) {
                 const double dd = __dsqrt_rn(__dadd_rn(cxy, sq(__dsub_rn(z, __ldg(zc + c)))));
                 if (dd < seed) seed = dd;
             }
@@ -132,17 +200,21 @@ __global__ void __launch_bounds__(256) map_nearest(MapDims g, ModelDev m, double
         const double T = seed > HIT ? seed : HIT;
         const double T2 = T * T * MARGIN;
         // 2. the reference's scan over the points that can still matter
+        const int2 xr = m.xsorted ? close_run(m.xm, m.mx, 1, x, T2) : make_int2(0, m.mx - 1);
+        const int2 yr = m.ysorted ? close_run(m.ym, m.my, 1, y, T2) : make_int2(0, m.my - 1);
         double ddmin = FAR;
         int64_t best = -1;
         bool hit = false;
-        for (int a = 0; a < m.mx && !hit; ++a) {
+        for (int a = xr.x; a <= xr.y && !hit; ++a) {
             const double cx = sq(__dsub_rn(x, __ldg(m.xm + a)));
             if (cx > T2) continue;
-            for (int b = 0; b < m.my && !hit; ++b) {
+            for (int b = yr.x; b <= yr.y && !hit; ++b) {
                 const double cxy = __dadd_rn(cx, sq(__dsub_rn(y, __ldg(m.ym + b))));
                 if (cxy > T2) continue;
                 const int64_t base = ((int64_t)a * m.my + b) * m.mz;
-                for (int c = 0; c < m.mz; ++c) {
+                const int dir = m.zsort[(int64_t)a * m.my + b];
+                const int2 zr = dir != 0 ? close_run(m.zm + base, m.mz, dir, z, T2) : make_int2(0, m.mz - 1);
+                for (int c = zr.x; c <= zr.y; ++c) {
                     const double s = __dadd_rn(cxy, sq(__dsub_rn(z, __ldg(m.zm + base + c))));
                     if (s > T2) continue;
                     const double dd = __dsqrt_rn(s);
@@ -349,7 +421,25 @@ extern "C" int mvf_map_model(const mvf_mesh *grid, const mvf_model *md, double o
         }
         if (e != cudaSuccess) return map_fail(MVF_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     }
-    DevBuf bxp, byp, bzp, bxm, bym, bzm, bsig, bmu, bs, bu, bv, berr;
+    // sortedness of the model's coordinate arrays (a NaN makes an array unsorted)
+    auto ascending = [](const double *v, int64_t n, int64_t stride) {
+        for (int64_t c = 0; c + 1 < n; ++c)
+            if (!(v[c * stride] <= v[(c + 1) * stride])) return false;
+        return true;
+    };
+    dm.xsorted = ascending(md->xm, md->mx, 1);
+    dm.ysorted = ascending(md->ym, md->my, 1);
+    std::vector<int8_t> zsort((size_t)md->mx * md->my);
+    for (int64_t col = 0; col < (int64_t)md->mx * md->my; ++col) {
+        const double *zc = md->zm + col * md->mz;
+        bool up = true, down = true;
+        for (int c = 0; c + 1 < md->mz && (up || down); ++c) {
+            if (!(zc[c] <= zc[c + 1])) up = false;
+            if (!(zc[c] >= zc[c + 1])) down = false;
+        }
+        zsort[col] = up ? 1 : down ? -1 : 0;
+    }
+    DevBuf bxp, byp, bzp, bxm, bym, bzm, bsig, bmu, bs, bu, bv, berr, bzs;
     auto alloc = [](DevBuf &b, size_t bytes) { return cudaMalloc(&b.p, std::max<size_t>(bytes, 16)); };
     auto put = [](DevBuf &b, const void *h, size_t bytes) {
         cudaError_t e = cudaMalloc(&b.p, std::max<size_t>(bytes, 16));
@@ -363,6 +453,7 @@ extern "C" int mvf_map_model(const mvf_mesh *grid, const mvf_model *md, double o
     if (e == cudaSuccess) e = put(bxm, md->xm, sizeof(double) * md->mx);
     if (e == cudaSuccess) e = put(bym, md->ym, sizeof(double) * md->my);
     if (e == cudaSuccess) e = put(bzm, md->zm, sizeof(double) * npts);
+    if (e == cudaSuccess) e = put(bzs, zsort.data(), zsort.size());
     if (e == cudaSuccess) e = put(bsig, md->sigma, sizeof(double) * msig);
     if (e == cudaSuccess && mmu) e = put(bmu, md->mu, sizeof(double) * mmu);
     if (e == cudaSuccess) e = alloc(bs, sizeof(double) * 12 * npt);
@@ -378,6 +469,7 @@ extern "C" int mvf_map_model(const mvf_mesh *grid, const mvf_model *md, double o
     dm.zm = (const double *)bzm.p;
     dm.sigma = (const double *)bsig.p;
     dm.mu = (const double *)bmu.p;
+    dm.zsort = (const int8_t *)bzs.p;
     double *sig = (double *)bs.p, *mu = (double *)bu.p;
     uint8_t *val = (uint8_t *)bv.p;
 

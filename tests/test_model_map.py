@@ -211,31 +211,70 @@ def test_oracle_map_semantics():
     assert np.array_equal(s[:, :, 0], s[:, :, E - 1])
 
 
+def _ascending(v):
+    return all(v[c] <= v[c + 1] for c in range(len(v) - 1))
+
+
+def _close_run(v, d, t, T2):
+    """close_run of mvf_model.cu: the run of sorted v (d = +1 ascending, -1 descending)
+    whose rounded squared difference to t is <= T2, by two bisections."""
+    n = len(v)
+    lo, hi = 0, n
+    while lo < hi:
+        c = (lo + hi) >> 1
+        past = v[c] >= t if d > 0 else v[c] <= t
+        if past or (t - v[c]) * (t - v[c]) <= T2:
+            hi = c
+        else:
+            lo = c + 1
+    first = lo
+    lo, hi = -1, n - 1
+    while lo < hi:
+        c = (lo + hi + 1) >> 1
+        before = v[c] <= t if d > 0 else v[c] >= t
+        if before or (t - v[c]) * (t - v[c]) <= T2:
+            lo = c
+        else:
+            hi = c - 1
+    return first, lo
+
+
 def _pruned(x, y, z, xm, ym, zm):
-    """The GPU kernel's scan (mvf_model.cu) in IEEE double: seed bound, then the
-    reference's comparisons on the points whose partial sums stay below T^2(1+1e-14)."""
+    """The GPU kernel's scan (mvf_model.cu) in IEEE double: seed bound, sorted runs found
+    by bisection, then the reference's comparisons on the points whose partial sums
+    stay below T^2(1+1e-14)."""
     mx, my, mz = zm.shape
-    ia = int(np.argmin(np.abs(x - xm)))
-    ja = int(np.argmin(np.abs(y - ym)))
-    cxy = (x - xm[ia]) ** 2 + (y - ym[ja]) ** 2
+    xm, ym = [float(v) for v in xm], [float(v) for v in ym]
+    zc = [[[float(v) for v in zm[a, b]] for b in range(my)] for a in range(mx)]
+    xs, ys = _ascending(xm), _ascending(ym)
+    zs = [[1 if _ascending(zc[a][b]) else -1 if _ascending(zc[a][b][::-1]) else 0 for b in range(my)]
+          for a in range(mx)]
+    ia = int(np.argmin(np.abs(x - np.array(xm))))
+    ja = int(np.argmin(np.abs(y - np.array(ym))))
+    cxy = (x - xm[ia]) * (x - xm[ia]) + (y - ym[ja]) * (y - ym[ja])
+    col = zc[ia][ja]
     seed = 1e20
     for c in range(mz):
-        dd = math.sqrt(cxy + (z - zm[ia, ja, c]) ** 2)
+        dd = math.sqrt(cxy + (z - col[c]) * (z - col[c]))
         if dd < seed:
             seed = dd
     T = max(seed, 1e-5)
     T2 = T * T * (1.0 + 1e-14)
+    xr = _close_run(xm, 1, x, T2) if xs else (0, mx - 1)
+    yr = _close_run(ym, 1, y, T2) if ys else (0, my - 1)
     ddmin, best = 1e20, -1
-    for a in range(mx):
-        cx = (x - xm[a]) ** 2
+    for a in range(xr[0], xr[1] + 1):
+        cx = (x - xm[a]) * (x - xm[a])
         if cx > T2:
             continue
-        for b in range(my):
-            cxy = cx + (y - ym[b]) ** 2
+        for b in range(yr[0], yr[1] + 1):
+            cxy = cx + (y - ym[b]) * (y - ym[b])
             if cxy > T2:
                 continue
-            for c in range(mz):
-                s = cxy + (z - zm[a, b, c]) ** 2
+            col = zc[a][b]
+            zr = _close_run(col, zs[a][b], z, T2) if zs[a][b] else (0, mz - 1)
+            for c in range(zr[0], zr[1] + 1):
+                s = cxy + (z - col[c]) * (z - col[c])
                 if s > T2:
                     continue
                 dd = math.sqrt(s)
@@ -263,16 +302,22 @@ def _brute(x, y, z, xm, ym, zm):
 def test_pruned_scan_picks_the_reference_point():
     """The kernel's pruning skips only points that can neither be within 1e-5 nor a new
     minimum: on lattices full of exact ties, duplicates, near-hits (just inside and
-    outside 1e-5) and unsorted coordinates it returns the brute-force scan's point."""
+    outside 1e-5), sorted (both directions) and unsorted coordinates it returns the
+    brute-force scan's point."""
     rng = np.random.Generator(np.random.PCG64(11))
-    for trial in range(60):
-        mx, my, mz = rng.integers(1, 6, 3)
+    for trial in range(120):
+        mx, my, mz = rng.integers(1, 7, 3)
         step = float(rng.choice([1.0, 0.5, 100.0, 1e-6]))
         xm = step * rng.integers(-3, 4, mx).astype(float)
         ym = step * rng.integers(-3, 4, my).astype(float)
         zm = step * rng.integers(-3, 4, (mx, my, mz)).astype(float)
         if trial % 3 == 1:
             xm += rng.uniform(-1, 1, mx) * step * 0.1
+        if trial % 2 == 0:  # sorted coordinates (duplicates kept), columns either way
+            xm, ym = np.sort(xm), np.sort(ym)
+            zm = np.sort(zm, axis=2)
+            if trial % 4 == 0:
+                zm = zm[:, :, ::-1].copy()
         for _ in range(20):
             x, y, z = (step * rng.integers(-4, 5, 3)).astype(float) / 2.0
             if trial % 4 == 2:
@@ -315,6 +360,28 @@ def test_gpu_map_ties_and_duplicates():
     # no node took a duplicate (the tripled values)
     vals = set(np.round(gm.sigma.reshape(-1), 15))
     assert set(np.round(s_g[:, 0].real[s_g[:, 0].real > 0], 15)) <= vals
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("layout", ["descending-columns", "unsorted"])
+def test_gpu_map_sorted_and_unsorted_model_arrays(layout):
+    """The kernel bisects sorted xm / ym / columns and scans unsorted ones in full; both
+    must give the oracle's (brute-force) answer bit for bit."""
+    from movfem_gb300 import api
+    m = small_grid(20, nextd=2, topo=25.0)
+    gm = M.synthetic_geomodel(13, m, spacing=70.0, depth=300.0, relief=20.0, anisotropic=True)
+    rng = np.random.Generator(np.random.PCG64(17))
+    if layout == "descending-columns":
+        gm.zm = gm.zm[:, :, ::-1].copy()
+    else:
+        gm.xm = gm.xm[rng.permutation(gm.xm.size)]
+        gm.ym = gm.ym[rng.permutation(gm.ym.size)]
+        gm.zm = np.take_along_axis(gm.zm, rng.permuted(np.argsort(gm.zm, axis=2), axis=2), axis=2)
+    w = 2 * math.pi * 0.3
+    s_o, u_o = oracle.map_model(m, gm, w)
+    s_g, u_g = api.map_model(m, gm, w)
+    assert np.array_equal(s_g.view(np.float64), s_o.view(np.float64))
+    assert np.array_equal(u_g, u_o)
 
 
 @pytest.mark.gpu
