@@ -133,14 +133,16 @@ class GeoModel:
         """Contiguous arrays for the C-ABI: ij tables in the Fortran layout
         {i_1..i_n, j_1..j_n}."""
         mx, my, mz = self.zm.shape
-        sig = np.ascontiguousarray(self.sigma, dtype=np.float64).reshape(mx * my * mz, -1)
-        ijs = np.ascontiguousarray(np.asarray(self.ijsigma, dtype=np.int32).reshape(-1, 2).T).reshape(-1)
+        ij_s = np.asarray(self.ijsigma, dtype=np.int32).reshape(-1, 2)
+        sig = np.ascontiguousarray(self.sigma, dtype=np.float64).reshape(mx * my * mz, ij_s.shape[0])
+        ijs = np.ascontiguousarray(ij_s.T).reshape(-1)
         if self.mu is None:
             mu, ijm, imu = None, None, 0
         else:
-            mu = np.ascontiguousarray(self.mu, dtype=np.float64).reshape(mx * my * mz, -1)
+            ij_m = np.asarray(self.ijmu, dtype=np.int32).reshape(-1, 2)
+            mu = np.ascontiguousarray(self.mu, dtype=np.float64).reshape(mx * my * mz, ij_m.shape[0])
             imu = mu.shape[1]
-            ijm = np.ascontiguousarray(np.asarray(self.ijmu, dtype=np.int32).reshape(-1, 2).T).reshape(-1)
+            ijm = np.ascontiguousarray(ij_m.T).reshape(-1)
         return dict(mx=mx, my=my, mz=mz, xm=np.ascontiguousarray(self.xm, dtype=np.float64),
                     ym=np.ascontiguousarray(self.ym, dtype=np.float64),
                     zm=np.ascontiguousarray(self.zm, dtype=np.float64).reshape(-1), isigma=sig.shape[1],

@@ -399,3 +399,36 @@ def test_gpu_map_rejects_what_the_reference_cannot_map():
     with pytest.raises(api.MVFError) as e:
         api.map_model(m0, gm, 1.0)
     assert e.value.code == api.E_ARG and "nextd" in str(e.value)
+
+
+def test_map_model_rejects_bad_arguments_before_any_device_work():
+    """mvf_map_model validates its arguments on the host before touching the GPU, so its
+    refusals (and their messages, through mvf_last_error(NULL)) are checked here
+    without one."""
+    from movfem_gb300 import api
+    m = small_grid(8, nextd=2)
+    gm = M.synthetic_geomodel(1, m, spacing=90.0, depth=300.0)
+    cases = []
+    m0 = small_grid(8, nextd=2)
+    m0.nextd = 0
+    cases.append((m0, gm, "nextd"))
+    m1 = small_grid(8, nextd=2)
+    m1.nzl_top = m1.nzl_air = 0
+    cases.append((m1, gm, "air"))
+    m2 = small_grid(8, nextd=2)
+    m2.nextd = 5  # nx = 9 elements: none left inside 2 x 5 extension cells
+    cases.append((m2, gm, "inner elements"))
+    bad_ij = M.GeoModel(xm=gm.xm, ym=gm.ym, zm=gm.zm, sigma=np.zeros((gm.zm.size, 2)),
+                        ijsigma=np.array([[1, 1], [0, 2]], dtype=np.int32))
+    cases.append((m, bad_ij, "ijsigma"))
+    empty = M.GeoModel(xm=gm.xm[:0], ym=gm.ym, zm=gm.zm[:0], sigma=np.zeros((0, 1)),
+                       ijsigma=np.array([[1, 1]], dtype=np.int32))
+    cases.append((m, empty, "empty"))
+    m3 = small_grid(8, nextd=2)
+    m3.nodes_per_elem = 9
+    cases.append((m3, gm, "nodes_per_elem"))
+    for grid, model, word in cases:
+        with pytest.raises(api.MVFError) as e:
+            api.map_model(grid, model, 1.0)
+        assert e.value.code == api.E_ARG, (word, e.value)
+        assert word in str(e.value), (word, str(e.value))
