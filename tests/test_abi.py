@@ -71,3 +71,47 @@ def test_model_struct_layout_matches_the_header():
         assert [f for f, _ in S._fields_] == fields
         assert out[0] == ctypes.sizeof(S)
         assert out[1:] == [getattr(S, f).offset for f in fields]
+
+
+def test_c_host_links_and_gets_errors_without_a_gpu():
+    """A plain C host (no Python) links libmovfem_gpu.so through include/movfem_gpu.h and
+    gets status codes and messages back from calls the library refuses before any
+    device work: the drop-in boundary as a C or Fortran caller sees it."""
+    import subprocess
+    import tempfile
+    lib = build.build()
+    libdir = os.path.dirname(lib)
+    cuda_lib = "/usr/local/cuda/lib64"
+    src = r'''
+#include <stdio.h>
+#include <string.h>
+#include "movfem_gpu.h"
+int main(void) {
+    mvf_ctx *ctx = 0;
+    mvf_mesh mesh;
+    mvf_model model;
+    double xp[2] = {0, 1}, sig[12], mu[6];
+    int rc;
+    memset(&mesh, 0, sizeof mesh);
+    memset(&model, 0, sizeof model);
+    if (mvf_create(&ctx, NULL, -1) != MVF_E_ARG) return 1;
+    if (mvf_map_model(NULL, &model, 1.0, sig, mu, NULL, -1) != MVF_E_ARG) return 2;
+    if (strstr(mvf_last_error(NULL), "null") == NULL) return 3;
+    mesh.nodes_per_elem = 8; mesh.nx = mesh.ny = mesh.nz = 1;
+    mesh.xp = mesh.yp = mesh.zp = xp;
+    mesh.nextd = 0;
+    rc = mvf_map_model(&mesh, &model, 1.0, sig, mu, NULL, -1);
+    if (rc != MVF_E_ARG || strstr(mvf_last_error(NULL), "nextd") == NULL) return 4;
+    printf("ok %d %s\n", rc, mvf_last_error(NULL));
+    return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "host.c")
+        exe = os.path.join(d, "host")
+        open(c, "w").write(src)
+        subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-I", HDR, c, "-o", exe, "-L", libdir,
+                               "-lmovfem_gpu", "-L", cuda_lib, "-lcudart", f"-Wl,-rpath,{libdir}:{cuda_lib}"])
+        out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
+    assert out.stdout.startswith("ok -1")
