@@ -8,8 +8,7 @@
  *   :115  call zmumps(mumps_par)              ! job=6: analyse + factor + solve, nrhs=2
  *   :123  call node_solution(mumps_par%rhs)   ! then receiver Z / rho / phi
  * with the numbering built once by ga_init (global_assembly.f90:26-41).  The entry
- * points below replace them; a Fortran host binds them with ISO_C_BINDING (see
- * INTEGRATION.md).  Plain pointers and sizes only; every function returns 0 on
+ * points below replace them; a Fortran host binds them with ISO_C_BINDING.  Plain pointers and sizes only; every function returns 0 on
  * success or a negative MVF_E_* code, and mvf_last_error() gives the message.
  * The library never calls back into the host, and one context is used by one host
  * thread at a time (the reference is single-threaded with module-level state).
@@ -139,6 +138,21 @@ int mvf_solve(mvf_ctx *ctx, double *rhs_inout, double tol, int32_t mode, int32_t
  * back to FP64 when a scaled inverse entry does not fit two FP32 halves).  The plain
  * FP64 mode always applies it in FP64.  0 keeps a setting. */
 int mvf_set_solver(mvf_ctx *ctx, int32_t restart, int32_t mixed_passes, int32_t patch_precision);
+/* Preconditioner of the 36/54-DOF systems (no counterpart in the reference, which
+ * factorises with MUMPS).  kind 0: multilevel (default): vertex-patch smoothing on the
+ * 36/54-DOF level, Galerkin coarsening to the 12-edge space on the same cells, then to
+ * merged cells, down to a directly solved level.  It works on K + i w Mp, where Mp is
+ * the mass matrix of the interpolated conductivity shifted positive semidefinite at
+ * every Gauss point plus a floor conductivity (S/m; default 1e-8, <= 0 keeps the
+ * setting) that makes the air's gradients regular.  kind 1: the one-level
+ * vertex-patch method.  Takes effect at the next mvf_assemble. */
+int mvf_set_preconditioner(mvf_ctx *ctx, int32_t kind, double tau);
+/* Levels of the multilevel preconditioner (0 when not in use) and the free DOFs of the
+ * first cap of them (level 0 is the system itself). */
+int mvf_mg_levels(const mvf_ctx *ctx, int32_t *nlevels, int32_t *ndofs, int32_t cap);
+/* Test hook: one cycle of the multilevel preconditioner for frequency f applied to R
+ * host right-hand sides r [n][R] complex; z [n][R] complex. */
+int mvf_mg_apply_once(mvf_ctx *ctx, int32_t f, int32_t R, const double *r, double *z);
 /* Arithmetic the last vertex-patch inversion set up: 0 no patches (12-DOF elements),
  * 1 FP64, 2 float-float (scaled inverses split into FP32 halves). */
 int32_t mvf_patch_arithmetic(const mvf_ctx *ctx);
@@ -201,13 +215,15 @@ int mvf_spmm_variant(mvf_ctx *ctx, int32_t f, int32_t variant, int32_t fp64, int
                      double *y);
 
 /* y = A_f x like mvf_spmv, for callers that cannot let the library allocate device
- * memory (a host whose device memory is owned by its own pool, or code between
- * captured / latency-critical stream steps).  No counterpart in the reference.
- * x, y: DEVICE pointers, [2][nne] complex.  Nothing is allocated: the staging lives
- * in a fixed 16 MiB device array shared by all calls, so nne must be <= 262144
- * (MVF_E_ARG otherwise) and calls that overlap on the GPU race on it.  The first
- * call on a device looks up that array's address; make it before any stream capture.
- * Returns after the result is in y. */
+ * memory (a host whose device memory is owned by its own pool allocator, where a
+ * cudaMalloc inside the library would fail or fragment that pool).  No counterpart in
+ * the reference.  x, y: DEVICE pointers, [2][nne] complex.  Nothing is allocated: the
+ * staging lives in a fixed 16 MiB device array shared by all calls, so nne must be
+ * <= 262144 (MVF_E_ARG otherwise) and calls that overlap on the GPU race on it.  The
+ * kernels run on the library's stream: x must be complete before the call (synchronise
+ * the stream that wrote it); the call synchronises that stream and returns with y
+ * complete.  The first call on a device looks up the array's device address and keeps
+ * it; no cudaDeviceReset may follow that first call in the process. */
 int mvf_spmv_noalloc(mvf_ctx *ctx, int32_t f, const double *x_dev, double *y_dev);
 
 /* Initial guess for the following mvf_solve calls (no counterpart in the reference:

@@ -140,15 +140,20 @@ struct Smem {
     double wgt[G::GC];
     double dk[G::GC][G::CW][G::CW];      // curl material matrix (times weight)
     double dm[G::GC][3][3];              // mass material matrix (times weight)
+    double dmp[G::GC][3][3];             // the same with |sigma| + floor (multilevel preconditioner)
     double srcw[G::GC][MVF_MAX_FREQ][2][6];  // weight*H*source, complex
     double bc[G::GC][ME][G::CW];
     double tc[G::GC][ME][G::CW];
     double bv[G::GC][ME][3];
     double tv[G::GC][ME][3];
+    double tvp[G::GC][ME][3];
     int gne[ME];
     int64_t node[MN];
     int err;
 };
+
+// local prolongation of the 12-edge space into this element's space (p_local)
+__constant__ PLoc c_ploc;
 
 template <int MN, int ME, int NGP, bool GPML>
 __global__ void __launch_bounds__(256) element_kernel(
@@ -160,7 +165,8 @@ __global__ void __launch_bounds__(256) element_kernel(
     const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col, double *__restrict__ K64,
     double *__restrict__ M64, double *__restrict__ rhs, int32_t nne, const int32_t *__restrict__ node_gidx,
     double *__restrict__ kphi, double *__restrict__ mphi, double *__restrict__ mabs, double *__restrict__ Kst,
-    double *__restrict__ Mst, double *__restrict__ bst, int64_t store_base, int *__restrict__ errflag) {
+    double *__restrict__ Mst, double *__restrict__ bst, int64_t store_base, int *__restrict__ errflag,
+    double *__restrict__ K1e, double *__restrict__ M1e, double *__restrict__ Mp64, double sfloor) {
     using G = Geom<MN, ME, NGP, GPML>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem<MN, ME, NGP, GPML> &S = *reinterpret_cast<Smem<MN, ME, NGP, GPML> *>(smem_raw);
@@ -238,9 +244,9 @@ __global__ void __launch_bounds__(256) element_kernel(
         }
         __syncthreads();
         // accumulators
-        double kacc[G::PPT], macc[G::PPT];
+        double kacc[G::PPT], macc[G::PPT], mpacc[G::PPT];
 #pragma unroll
-        for (int q = 0; q < G::PPT; ++q) kacc[q] = macc[q] = 0.0;
+        for (int q = 0; q < G::PPT; ++q) kacc[q] = macc[q] = mpacc[q] = 0.0;
         constexpr int NB = ME * 2 * MVF_MAX_FREQ;
         constexpr int BPT = (ME * 2 + 255) / 256;  // (edge, pol) slots per thread per frequency
         double bacc[BPT][MVF_MAX_FREQ][2];
@@ -296,6 +302,23 @@ __global__ void __launch_bounds__(256) element_kernel(
                 // mass material matrix: Re(H sigma) (f2, integration.f90:211-238)
                 for (int a = 0; a < 3; ++a)
                     for (int b = 0; b < 3; ++b) S.dm[gl][a][b] = w * cmul(H, mf2[pk(a, b)]).re;
+                if (K1e) {
+                    // the multilevel preconditioner's conductivity: the interpolated real
+                    // part, shifted to be positive semidefinite where the quadratic
+                    // interpolation of a jump undershoots (|sigma| for an isotropic one),
+                    // plus a floor that makes the air's gradients regular
+                    double gmin = 1e300;
+                    for (int a = 0; a < 3; ++a) {
+                        double off = 0.0;
+                        for (int b = 0; b < 3; ++b)
+                            if (b != a) off += fabs(mf2[pk(a, b)].re);
+                        gmin = fmin(gmin, mf2[pk(a, a)].re - off);
+                    }
+                    const double shift = 2.0 * fmax(0.0, -gmin) + sfloor;
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b)
+                            S.dmp[gl][a][b] = w * (cmul(H, mf2[pk(a, b)]).re + (a == b ? H.re * shift : 0.0));
+                }
                 // curl material matrix (f1, integration.f90:154-209)
                 if (GPML) {
                     // partial (c,p) is a derivative along axis ax[c][p]
@@ -398,6 +421,9 @@ __global__ void __launch_bounds__(256) element_kernel(
                 for (int a = 0; a < 3; ++a) ve[a] = L * vij[a];
                 for (int a = 0; a < 3; ++a) S.bv[gl][j][a] = ve[a];
                 for (int a = 0; a < 3; ++a) S.tv[gl][j][a] = S.dm[gl][a][0] * ve[0] + S.dm[gl][a][1] * ve[1] + S.dm[gl][a][2] * ve[2];
+                if (K1e)
+                    for (int a = 0; a < 3; ++a)
+                        S.tvp[gl][j][a] = S.dmp[gl][a][0] * ve[0] + S.dmp[gl][a][1] * ve[1] + S.dmp[gl][a][2] * ve[2];
             }
             __syncthreads();
             // ---- accumulate K_e, M_e (alocal) and b_e (blocal)
@@ -410,15 +436,20 @@ __global__ void __launch_bounds__(256) element_kernel(
                     while ((i + 1) * (i + 2) / 2 <= p) ++i;
                     while (i * (i + 1) / 2 > p) --i;
                     const int jj = p - i * (i + 1) / 2;  // jj <= i
-                    double ks = 0.0, ms = 0.0;
+                    double ks = 0.0, ms = 0.0, mps = 0.0;
                     for (int gl = 0; gl < G::GC; ++gl) {
 #pragma unroll
                         for (int r = 0; r < G::CW; ++r) ks += S.bc[gl][i][r] * S.tc[gl][jj][r];
 #pragma unroll
                         for (int r = 0; r < 3; ++r) ms += S.bv[gl][i][r] * S.tv[gl][jj][r];
+                        if (K1e) {
+#pragma unroll
+                            for (int r = 0; r < 3; ++r) mps += S.bv[gl][i][r] * S.tvp[gl][jj][r];
+                        }
                     }
                     kacc[q] += ks;
                     macc[q] += ms;
+                    mpacc[q] += mps;
                 }
             }
 #pragma unroll
@@ -575,12 +606,63 @@ __global__ void __launch_bounds__(256) element_kernel(
             mabs[gn] += ma;
         }
         __syncthreads();
+        if constexpr (ME != 12) {
+            if (K1e) {
+                // the preconditioner's element mass replaces M_e in shared memory; then the
+                // Galerkin element matrices on the 12-edge space of the same cell,
+                // P^T K_e P and P^T Mp_e P, and the scatter of Mp_e into the preconditioner's
+                // CSR values
+#pragma unroll
+                for (int q = 0; q < G::PPT; ++q) {
+                    const int p = tid + q * 256;
+                    if (p < G::NPAIR) {
+                        int i = (int)((sqrt(8.0 * p + 1.0) - 1.0) * 0.5);
+                        while ((i + 1) * (i + 2) / 2 <= p) ++i;
+                        while (i * (i + 1) / 2 > p) --i;
+                        const int jj = p - i * (i + 1) / 2;
+                        Ms[i * ME + jj] = mpacc[q];
+                        Ms[jj * ME + i] = mpacc[q];
+                    }
+                }
+                __syncthreads();
+                for (int t = tid; t < 144; t += blockDim.x) {
+                    const int a = t / 12, b = t % 12;
+                    double k = 0.0, mm = 0.0;
+                    for (int p = 0; p < c_ploc.cnt[a]; ++p) {
+                        const int i = c_ploc.idx[a][p];
+                        const double pa = c_ploc.val[a][p];
+                        for (int q = 0; q < c_ploc.cnt[b]; ++q) {
+                            const int j = c_ploc.idx[b][q];
+                            const double w = pa * c_ploc.val[b][q];
+                            k += w * Ks[i * ME + j];
+                            mm += w * Ms[i * ME + j];
+                        }
+                    }
+                    K1e[e * 144 + t] = k;
+                    M1e[e * 144 + t] = mm;
+                }
+                for (int t = tid; t < ME * ME; t += blockDim.x) {
+                    const int i = t / ME, j = t % ME;
+                    const int gi = S.gne[i], gj = S.gne[j];
+                    if (gi <= 0 || gj <= 0) continue;
+                    int64_t lo = rowptr[gi - 1], hi = rowptr[gi] - 1;
+                    while (lo < hi) {
+                        const int64_t mid = (lo + hi) >> 1;
+                        if (col[mid] < gj - 1) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    if (col[lo] == gj - 1) Mp64[lo] += Ms[t];
+                }
+                __syncthreads();
+            }
+        }
     }
 }
 
 template <int MN, int ME, int NGP, bool GPML>
 static int launch_elements(Ctx *c, MatrixSet &S, const int32_t *elems, int64_t n, double *Kst, double *Mst, double *bst,
                            int64_t store_base, int *errflag) {
+    double *K1e = Kst ? nullptr : S.K1e, *M1e = Kst ? nullptr : S.M1e, *Mp64 = Kst ? nullptr : S.Mp64;
     using SM = Smem<MN, ME, NGP, GPML>;
     const size_t smem = sizeof(SM);
     auto kern = element_kernel<MN, ME, NGP, GPML>;
@@ -591,7 +673,7 @@ static int launch_elements(Ctx *c, MatrixSet &S, const int32_t *elems, int64_t n
     kern<<<(unsigned)grid, 256, smem, c->stream>>>(
         elems, n, c->d.xp, c->d.yp, c->d.zp, c->d.sigma, c->d.sigma_f, c->d.mu, c->d.gne, c->d.N, c->d.dN, c->d.L,
         c->d.dL, c->d.gp, c->d.edge_node, c->d.edge_dir, c->d.rowptr, c->d.col, S.K64, S.M64, c->d.rhs, c->nne,
-        c->d.node_gidx, S.kphi, S.mphi, S.mabs, Kst, Mst, bst, store_base, errflag);
+        c->d.node_gidx, S.kphi, S.mphi, S.mabs, Kst, Mst, bst, store_base, errflag, K1e, M1e, Mp64, c->mg_floor);
     MVF_CUDA(c, cudaGetLastError());
     return 0;
 }
@@ -685,7 +767,7 @@ static int upload_glist(Ctx *c) {
 
 void free_sets(Ctx *c) {
     for (MatrixSet &S : c->sets) {
-        void *p[] = {S.K64, S.M64, S.K32, S.M32, S.kphi, S.mphi, S.mabs, S.Kff, S.Mff};
+        void *p[] = {S.K64, S.M64, S.K32, S.M32, S.kphi, S.mphi, S.mabs, S.Kff, S.Mff, S.K1e, S.M1e, S.Mp64};
         for (void *q : p)
             if (q) cudaFree(q);
     }
@@ -707,6 +789,15 @@ int assemble_set(Ctx *c, MatrixSet &S, bool gpml, int fset) {
     MVF_CUDA(c, cudaMemsetAsync(S.kphi, 0, std::max<int64_t>(c->ngn, 1) * sizeof(double), c->stream));
     MVF_CUDA(c, cudaMemsetAsync(S.mphi, 0, std::max<int64_t>(c->ngn, 1) * sizeof(double), c->stream));
     MVF_CUDA(c, cudaMemsetAsync(S.mabs, 0, std::max<int64_t>(c->ngn, 1) * sizeof(double), c->stream));
+    if (c->use_patches && c->precond == 0 && !c->mg.empty()) {
+        MVF_CUDA(c, cudaMalloc((void **)&S.K1e, (size_t)c->ne * 144 * sizeof(double)));
+        MVF_CUDA(c, cudaMalloc((void **)&S.M1e, (size_t)c->ne * 144 * sizeof(double)));
+        MVF_CUDA(c, cudaMalloc((void **)&S.Mp64, nnz * sizeof(double)));
+        MVF_CUDA(c, cudaMemsetAsync(S.Mp64, 0, nnz * sizeof(double), c->stream));
+        PLoc pl;
+        p_local(c->T.mn, pl);
+        MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_ploc, &pl, sizeof pl, 0, cudaMemcpyHostToDevice, c->stream));
+    }
     AsmParams ap;
     set_params(c, ap, fset, S.nfreq, c->omega + S.first_freq, gpml, c->ifreq0 + S.first_freq);
     MVF_CUDA(c, cudaMemcpyToSymbolAsync(c_ap, &ap, sizeof ap, 0, cudaMemcpyHostToDevice, c->stream));

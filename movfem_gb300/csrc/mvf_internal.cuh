@@ -17,6 +17,7 @@
 #define MVF_MAX_ME 54
 #define MVF_MAX_GP 27
 #define MVF_MAX_FREQ 16
+#define MVF_MG_MAXP 96  // largest direct-solved coarsest level of the multilevel preconditioner
 
 namespace mvf {
 
@@ -43,8 +44,50 @@ struct MatrixSet {
     double *K64 = nullptr, *M64 = nullptr;  // [nnz]
     float *K32 = nullptr, *M32 = nullptr;   // [nnz]
     float2 *Kff = nullptr, *Mff = nullptr;  // [nnz] FP64 values as hi + lo FP32 halves (made on demand)
+    // multilevel preconditioner: its mass matrix Mp (conductivity |sigma| + floor at
+    // every Gauss point) [nnz], and the Galerkin element matrices on the lowest-order
+    // edge space of the same cells, P^T K_e P and P^T Mp_e P, [ne][12][12]
+    double *Mp64 = nullptr;
+    double *K1e = nullptr, *M1e = nullptr;
     double *kphi = nullptr, *mphi = nullptr, *mabs = nullptr;  // gradient-node diagonals [ngn]
     int first_freq = 0, nfreq = 0;          // frequencies that use this set
+};
+
+// Vertex patches of one grid level (host lists; see vertex_patches).
+struct PatchHost {
+    std::vector<int64_t> ptr, ioff, color_off;  // [np+1], [np+1], [9]
+    std::vector<int32_t> dof;
+    int pmax = 0;
+};
+
+// One level of the multilevel preconditioner below the 36/54-DOF system: the
+// lowest-order (12-edge) space on a cell grid.  Level 1 has the context's cells,
+// level l+1 merges the cells of level l in pairs along each axis.
+struct MgLevel {
+    int nx = 0, ny = 0, nz = 0;    // cells
+    int32_t n = 0;                 // free DOFs
+    int64_t ne = 0, nnz = 0;
+    std::vector<int32_t> gne;      // [ne][12], 1-based, <= 0 eliminated
+    std::vector<int> ix, iy, iz;   // this level's vertices as vertex indices of the finer level
+    int64_t *rowptr = nullptr;     // CSR pattern (both triangles)
+    int32_t *col = nullptr;
+    int32_t *gne_d = nullptr;
+    // prolongation to the next finer level (P: [n_fine][n]) and its transpose
+    int64_t *prow = nullptr, *ptrow = nullptr;
+    int32_t *pcol = nullptr, *ptcol = nullptr;
+    double *pval = nullptr, *ptval = nullptr;
+    // levels >= 2: the finer-level children of each element and the local maps
+    // Q [ne][8][12 fine][12 this] (child -1: none)
+    int32_t *child = nullptr;
+    double *Q = nullptr;
+    std::vector<int64_t> ecolor_off;  // [9] offsets of the parity colours in elist
+    int32_t *elist = nullptr;
+    // vertex patches (the coarsest level: one patch holding every DOF)
+    int64_t np = 0, pent = 0;
+    int pmax = 0;
+    std::vector<int64_t> pcolor_off;  // [9]
+    int64_t *pptr = nullptr, *pioff = nullptr;
+    int32_t *pdof = nullptr;
 };
 
 struct Device {
@@ -127,6 +170,12 @@ struct Ctx {
     // whether the inverses of the last inversion were split into FP32 halves
     int patch_precision = 2, patch_inv_split = 0;
     int solve_mode = 0;  // mode of the solve in progress (1: plain FP64 throughout)
+    // preconditioner of the 36/54-DOF systems: 0 multilevel (default), 1 one-level
+    // vertex patches; multilevel hierarchy (levels 1..) and the conductivity floor
+    // (S/m) of its operator
+    int precond = 0;
+    double mg_floor = 1e-8;
+    std::vector<MgLevel> mg;
 };
 
 // process-wide count of the library's kernel launches.  While a thread captures a
@@ -170,11 +219,36 @@ void free_sets(Ctx *c);
 // message of this thread's last context-free call (mvf_map_model, mvf_model.cu)
 const char *map_last_error();
 
+// numbering and pattern of an element grid (mvf_setup.cu)
+int32_t number_grid(const OrderTables &T, int nx, int ny, int nz, bool dirichlet, std::vector<int32_t> &gne);
+void pattern_from_gne(const std::vector<int32_t> &gne, int me, int64_t ne, int32_t n, std::vector<int64_t> &rowptr,
+                      std::vector<int32_t> &col);
+
 // vertex-patch Schwarz preconditioner (mvf_patch.cu)
+void vertex_patches(int nx, int ny, int nz, int me, const std::vector<int32_t> &gne, int32_t n, PatchHost &out);
+void launch_patch_invert(cudaStream_t st, int grid, int64_t np, const int64_t *pptr, const int32_t *pdof,
+                         const int64_t *ioff, const int64_t *rowptr, const int32_t *col, const double *K,
+                         const double *M, double w, double tau, int pmax, double2 *ws, double2 *inv, int *err);
 int patch_setup(Ctx *c);
 int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **inv_out);
 void patch_apply(Ctx *c, const double2 *inv, int R, int npol, int nfi, const float2 *r, float2 *z);
 void patch_apply(Ctx *c, const double2 *inv, int R, int npol, int nfi, const double2 *r, double2 *z);
+
+// multilevel preconditioner (mvf_mg.cu)
+int mg_setup(Ctx *c);          // hierarchy, once per context
+void mg_release(Ctx *c);
+struct MgWork;                  // numeric state of one solve batch
+int mg_numeric(Ctx *c, const MatrixSet &S, const double *w, int nf, int R, int npol, MgWork **out);
+void mg_apply(Ctx *c, MgWork *W, const double2 *r, double2 *z);
+void mg_free(Ctx *c, MgWork *W);
+// local prolongation of the 12-edge element into the 36/54-DOF element: lists per
+// 12-edge DOF a of (36/54-DOF index, coefficient); count per a
+struct PLoc {
+    int cnt[12];
+    int idx[12][8];
+    double val[12][8];
+};
+void p_local(int mn, PLoc &P);
 
 }  // namespace mvf
 

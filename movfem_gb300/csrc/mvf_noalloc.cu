@@ -3,10 +3,10 @@
 // mvf_spmv (the parity hook) stages the two polarisations in an interleaved
 // [row][polarisation] layout in buffers it allocates on every call.  Some callers
 // cannot let a library allocate: a host that has handed the whole device-memory
-// budget to its own pool allocator, or code that runs between the steps of a
-// captured or latency-critical stream sequence, where cudaMalloc/cudaFree would
-// synchronise the device or fail.  mvf_spmv_noalloc does the same product with the
-// staging buffers in a fixed, file-scope device array instead.
+// budget to its own pool allocator (a Fortran or C++ solver framework that owns the
+// device), where a cudaMalloc from inside the library would fail or fragment that
+// pool.  mvf_spmv_noalloc does the same product with the staging buffers in a fixed,
+// file-scope device array instead.
 //
 // Limits and sharing rules:
 //  * at most MVF_NOALLOC_MAX_DOF free DOFs (the array holds two [nne][2] complex
@@ -14,9 +14,13 @@
 //  * all calls share the array; each call writes every word it reads before reading
 //    it, so nothing carries over from the previous call, but two calls whose kernels
 //    overlap on the GPU (different streams or contexts on one device) race on it;
+//  * the kernels run on the library's own stream: the caller must have finished
+//    writing x_dev (synchronise the stream or event that produced it) before the
+//    call, and the call synchronises the library's stream before it returns, so y_dev
+//    is complete when it does;
 //  * the first call on a device looks up the array's device address (once per device,
-//    with that device current) and caches it; make that first call before any stream
-//    capture that contains later calls.
+//    with that device current) and caches it; a cudaDeviceReset after that first call
+//    invalidates the cached address, so no device reset may follow it in the process.
 #include <cstdio>
 #include <mutex>
 
@@ -111,6 +115,8 @@ extern "C" int mvf_spmv_noalloc(mvf_ctx *xc, int32_t f, const double *x_dev, dou
     const MatrixSet *S = nullptr;
     for (const MatrixSet &s : c->sets)
         if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
+    if (!S) return fail(c, MVF_E_STATE, "no assembled matrix set holds this frequency");
+    if (c->nne == 0) return 0;
     double2 *scratch = nullptr;
     int rc = scratch_for(c, &scratch);
     if (rc) return rc;

@@ -22,11 +22,11 @@
 
 namespace mvf {
 
-// Build the patch lists (host, once per context).
-int patch_setup(Ctx *c) {
-    const int me = c->T.me;
-    const int nx = c->mesh.nx, ny = c->mesh.ny, nz = c->mesh.nz;
-    const int32_t n = c->nne;
+// Vertex patches of an element grid with numbering gne ([ne][me], 1-based, <= 0 for
+// eliminated DOFs): a DOF lies in the patch of vertex v when every element that holds it
+// lies in the 2x2x2 block of elements around v.  Patches are ordered by vertex-parity
+// colour; empty ones are dropped.
+void vertex_patches(int nx, int ny, int nz, int me, const std::vector<int32_t> &gne, int32_t n, PatchHost &out) {
     std::vector<int32_t> lo(3 * (size_t)n, INT32_MAX), hi(3 * (size_t)n, -1);
     for (int ie = 0; ie < nx; ++ie)
         for (int je = 0; je < ny; ++je)
@@ -34,7 +34,7 @@ int patch_setup(Ctx *c) {
                 const int64_t e = ((int64_t)ie * ny + je) * nz + ke;
                 const int idx[3] = {ie, je, ke};
                 for (int j = 0; j < me; ++j) {
-                    const int32_t g = c->gne_h[(size_t)e * me + j];
+                    const int32_t g = gne[(size_t)e * me + j];
                     if (g <= 0) continue;
                     for (int a = 0; a < 3; ++a) {
                         lo[3 * (size_t)(g - 1) + a] = std::min(lo[3 * (size_t)(g - 1) + a], idx[a]);
@@ -56,12 +56,11 @@ int patch_setup(Ctx *c) {
                 for (int vk = a0[2]; vk <= a1[2]; ++vk) fn(((int64_t)vi * nvy + vj) * nvz + vk);
     };
     for (int32_t g = 0; g < n; ++g) for_patches(g, [&](int64_t v) { cnt[v]++; });
-    // order patches by colour (vertex parity), drop empty ones
     std::vector<int64_t> order;
     order.reserve(nv);
-    c->pcolor_off.assign(9, 0);
+    out.color_off.assign(9, 0);
     for (int col = 0; col < 8; ++col) {
-        c->pcolor_off[col] = (int64_t)order.size();
+        out.color_off[col] = (int64_t)order.size();
         for (int64_t vi = col & 1; vi < nvx; vi += 2)
             for (int64_t vj = (col >> 1) & 1; vj < nvy; vj += 2)
                 for (int64_t vk = (col >> 2) & 1; vk < nvz; vk += 2) {
@@ -69,32 +68,40 @@ int patch_setup(Ctx *c) {
                     if (cnt[v] > 0) order.push_back(v);
                 }
     }
-    c->pcolor_off[8] = (int64_t)order.size();
+    out.color_off[8] = (int64_t)order.size();
     const int64_t np = (int64_t)order.size();
     std::vector<int64_t> slot(nv, -1);
     for (int64_t p = 0; p < np; ++p) slot[order[p]] = p;
-    std::vector<int64_t> ptr(np + 1, 0);
-    for (int64_t p = 0; p < np; ++p) ptr[p + 1] = ptr[p] + cnt[order[p]];
-    std::vector<int32_t> dof(ptr[np]);
-    std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
-    for (int32_t g = 0; g < n; ++g) for_patches(g, [&](int64_t v) { dof[fill[slot[v]]++] = g; });
-    int pmax = 0;
-    std::vector<int64_t> ioff(np + 1, 0);
+    out.ptr.assign(np + 1, 0);
+    for (int64_t p = 0; p < np; ++p) out.ptr[p + 1] = out.ptr[p] + cnt[order[p]];
+    out.dof.assign(out.ptr[np], 0);
+    std::vector<int64_t> fill(out.ptr.begin(), out.ptr.end() - 1);
+    for (int32_t g = 0; g < n; ++g) for_patches(g, [&](int64_t v) { out.dof[fill[slot[v]]++] = g; });
+    out.pmax = 0;
+    out.ioff.assign(np + 1, 0);
     for (int64_t p = 0; p < np; ++p) {
-        const int sz = (int)(ptr[p + 1] - ptr[p]);
-        pmax = std::max(pmax, sz);
-        ioff[p + 1] = ioff[p] + (int64_t)sz * sz;
+        const int sz = (int)(out.ptr[p + 1] - out.ptr[p]);
+        out.pmax = std::max(out.pmax, sz);
+        out.ioff[p + 1] = out.ioff[p] + (int64_t)sz * sz;
     }
+}
+
+// Build the patch lists of the context's own grid (host, once per context).
+int patch_setup(Ctx *c) {
+    PatchHost h;
+    vertex_patches(c->mesh.nx, c->mesh.ny, c->mesh.nz, c->T.me, c->gne_h, c->nne, h);
+    const int64_t np = (int64_t)h.ptr.size() - 1;
+    c->pcolor_off = h.color_off;
     c->npatch = np;
-    c->patch_max = pmax;
-    c->patch_entries = ioff[np];
-    c->patch_dofs = ptr[np];
+    c->patch_max = h.pmax;
+    c->patch_entries = h.ioff[np];
+    c->patch_dofs = h.ptr[np];
     MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_ptr, (np + 1) * sizeof(int64_t)));
-    MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_dof, std::max<int64_t>(ptr[np], 1) * sizeof(int32_t)));
+    MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_dof, std::max<int64_t>(h.ptr[np], 1) * sizeof(int32_t)));
     MVF_CUDA(c, cudaMalloc((void **)&c->d.patch_ioff, (np + 1) * sizeof(int64_t)));
-    MVF_CUDA(c, cudaMemcpy(c->d.patch_ptr, ptr.data(), (np + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-    MVF_CUDA(c, cudaMemcpy(c->d.patch_dof, dof.data(), ptr[np] * sizeof(int32_t), cudaMemcpyHostToDevice));
-    MVF_CUDA(c, cudaMemcpy(c->d.patch_ioff, ioff.data(), (np + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    MVF_CUDA(c, cudaMemcpy(c->d.patch_ptr, h.ptr.data(), (np + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    MVF_CUDA(c, cudaMemcpy(c->d.patch_dof, h.dof.data(), h.ptr[np] * sizeof(int32_t), cudaMemcpyHostToDevice));
+    MVF_CUDA(c, cudaMemcpy(c->d.patch_ioff, h.ioff.data(), (np + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
     return 0;
 }
 
@@ -104,8 +111,8 @@ int patch_setup(Ctx *c) {
 __global__ void __launch_bounds__(256) patch_invert_kernel(
     int64_t np, const int64_t *__restrict__ pptr, const int32_t *__restrict__ pdof, const int64_t *__restrict__ ioff,
     const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col, const double *__restrict__ K,
-    const double *__restrict__ M, double w, int pmax, double2 *__restrict__ ws_all, double2 *__restrict__ inv,
-    int *__restrict__ err) {
+    const double *__restrict__ M, double w, double tau, int pmax, double2 *__restrict__ ws_all,
+    double2 *__restrict__ inv, int *__restrict__ err) {
     __shared__ int piv_row;
     __shared__ double red_v[256];
     __shared__ int red_i[256];
@@ -130,8 +137,12 @@ __global__ void __launch_bounds__(256) patch_invert_kernel(
             ws[i * W2 + P + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
         }
         __syncthreads();
-        // shift: 1e-10 of the largest diagonal modulus
-        if (threadIdx.x == 0) {
+        // tau > 0: the regularised operator K + i w (M + tau diag K) of the multilevel
+        // preconditioner; tau == 0: the operator as it is; tau < 0: a real shift of
+        // 1e-10 of the largest diagonal modulus (the one-level preconditioner)
+        if (tau > 0.0) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) ws[i * W2 + i].y += w * tau * ws[i * W2 + i].x;
+        } else if (tau < 0.0 && threadIdx.x == 0) {
             double dmax = 0.0;
             for (int i = 0; i < P; ++i) dmax = fmax(dmax, hypot(ws[i * W2 + i].x, ws[i * W2 + i].y));
             const double s = 1e-10 * dmax;
@@ -200,6 +211,14 @@ __global__ void __launch_bounds__(256) patch_invert_kernel(
         }
         __syncthreads();
     }
+}
+
+// Inverses of the patches of one grid level for one frequency (see the kernel above).
+void launch_patch_invert(cudaStream_t st, int grid, int64_t np, const int64_t *pptr, const int32_t *pdof,
+                         const int64_t *ioff, const int64_t *rowptr, const int32_t *col, const double *K,
+                         const double *M, double w, double tau, int pmax, double2 *ws, double2 *inv, int *err) {
+    count_launch();
+    patch_invert_kernel<<<grid, 256, 0, st>>>(np, pptr, pdof, ioff, rowptr, col, K, M, w, tau, pmax, ws, inv, err);
 }
 
 // z[dof][r] += A_v^-1 r[dof][r] for the patches [p0, p1) (one colour); the inverse of
@@ -388,7 +407,7 @@ int patch_invert(Ctx *c, const MatrixSet &S, const double *w, int nf, double2 **
     for (int f = 0; f < nf; ++f) {
         count_launch();
         patch_invert_kernel<<<grid, 256, 0, c->stream>>>(c->npatch, c->d.patch_ptr, c->d.patch_dof, c->d.patch_ioff,
-                                                          c->d.rowptr, c->d.col, S.K64, S.M64, w[f], c->patch_max, ws,
+                                                          c->d.rowptr, c->d.col, S.K64, S.M64, w[f], -1.0, c->patch_max, ws,
                                                           inv + (int64_t)f * ent, err);
     }
     MVF_CUDA(c, cudaGetLastError());

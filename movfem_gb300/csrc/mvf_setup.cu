@@ -179,10 +179,9 @@ void build_tables(int mn, int quirks, OrderTables &T) {
 // neighbours in that order; in Dirichlet mode, a DOF on the domain boundary gets the
 // negative number of the first boundary face (x-, y-, z-, x+, y+, z+) it lies on; every
 // other new DOF is numbered in element order.
-static int32_t number_dofs(const Ctx &c, std::vector<int32_t> &gne) {
-    const OrderTables &T = c.T;
-    const int me = T.me, nx = c.mesh.nx, ny = c.mesh.ny, nz = c.mesh.nz;
-    gne.assign((size_t)c.ne * me, 0);
+int32_t number_grid(const OrderTables &T, int nx, int ny, int nz, bool dirichlet, std::vector<int32_t> &gne) {
+    const int me = T.me;
+    gne.assign((size_t)nx * ny * nz * me, 0);
     int32_t next = 0;
     std::vector<char> face_of[6];  // membership per boundary face
     for (int f = 0; f < 6; ++f) face_of[f].assign(me, 0);
@@ -208,7 +207,7 @@ static int32_t number_dofs(const Ctx &c, std::vector<int32_t> &gne) {
                 const bool onb[6] = {ie == 0, je == 0, ke == 0, ie == nx - 1, je == ny - 1, ke == nz - 1};
                 for (int j = 0; j < me; ++j) {
                     int face = 0;
-                    if (c.mesh.dirichlet)
+                    if (dirichlet)
                         for (int f = 0; f < 6 && !face; ++f)
                             if (onb[f] && face_of[f][j]) face = f + 1;
                     if (face) row[j] = -face;
@@ -220,23 +219,26 @@ static int32_t number_dofs(const Ctx &c, std::vector<int32_t> &gne) {
     return nne;
 }
 
+static int32_t number_dofs(const Ctx &c, std::vector<int32_t> &gne) {
+    return number_grid(c.T, c.mesh.nx, c.mesh.ny, c.mesh.nz, c.mesh.dirichlet != 0, gne);
+}
+
 // Full symmetric CSR pattern: row r holds every free DOF that shares an element with r.
-static void build_pattern(const Ctx &c, std::vector<int64_t> &rowptr, std::vector<int32_t> &col) {
-    const int me = c.T.me;
-    const int32_t n = c.nne;
+void pattern_from_gne(const std::vector<int32_t> &gne, int me, int64_t ne, int32_t n, std::vector<int64_t> &rowptr,
+                      std::vector<int32_t> &col) {
     std::vector<int64_t> deg(n + 1, 0);
-    for (int64_t e = 0; e < c.ne; ++e)
+    for (int64_t e = 0; e < ne; ++e)
         for (int j = 0; j < me; ++j) {
-            const int32_t g = c.gne_h[(size_t)e * me + j];
+            const int32_t g = gne[(size_t)e * me + j];
             if (g > 0) deg[g]++;
         }
     std::vector<int64_t> ip(n + 1, 0);
     for (int32_t r = 0; r < n; ++r) ip[r + 1] = ip[r] + deg[r + 1];
     std::vector<int64_t> elist(ip[n]);
     std::vector<int64_t> fill(ip.begin(), ip.end() - 1);
-    for (int64_t e = 0; e < c.ne; ++e)
+    for (int64_t e = 0; e < ne; ++e)
         for (int j = 0; j < me; ++j) {
-            const int32_t g = c.gne_h[(size_t)e * me + j];
+            const int32_t g = gne[(size_t)e * me + j];
             if (g > 0) elist[fill[g - 1]++] = e;
         }
     rowptr.assign(n + 1, 0);
@@ -248,7 +250,7 @@ static void build_pattern(const Ctx &c, std::vector<int64_t> &rowptr, std::vecto
         for (int32_t r = 0; r < n; ++r) {
             buf.clear();
             for (int64_t k = ip[r]; k < ip[r + 1]; ++k) {
-                const int32_t *row = &c.gne_h[(size_t)elist[k] * me];
+                const int32_t *row = &gne[(size_t)elist[k] * me];
                 for (int j = 0; j < me; ++j)
                     if (row[j] > 0) buf.push_back(row[j] - 1);
             }
@@ -265,7 +267,7 @@ static void build_pattern(const Ctx &c, std::vector<int64_t> &rowptr, std::vecto
         for (int32_t r = 0; r < n; ++r) {
             buf.clear();
             for (int64_t k = ip[r]; k < ip[r + 1]; ++k) {
-                const int32_t *row = &c.gne_h[(size_t)elist[k] * me];
+                const int32_t *row = &gne[(size_t)elist[k] * me];
                 for (int j = 0; j < me; ++j)
                     if (row[j] > 0) buf.push_back(row[j] - 1);
             }
@@ -274,6 +276,10 @@ static void build_pattern(const Ctx &c, std::vector<int64_t> &rowptr, std::vecto
             std::copy(buf.begin(), end, col.begin() + rowptr[r]);
         }
     }
+}
+
+static void build_pattern(const Ctx &c, std::vector<int64_t> &rowptr, std::vector<int32_t> &col) {
+    pattern_from_gne(c.gne_h, c.T.me, c.ne, c.nne, rowptr, col);
 }
 
 template <class T>
@@ -485,11 +491,13 @@ static int create(Ctx *c, const mvf_mesh *m, int device) {
     // the 36- and 54-DOF elements are preconditioned with vertex patches
     c->use_patches = c->T.mn != 8;
     if (c->use_patches && (rc = patch_setup(c))) return rc;
+    if (c->use_patches && c->precond == 0 && (rc = mg_setup(c))) return rc;
     return 0;
 }
 
 static void release(Ctx *c) {
     free_sets(c);
+    mg_release(c);
     void *ptrs[] = {c->d.xp, c->d.yp, c->d.zp, c->d.sigma, c->d.sigma_f, c->d.mu, c->d.gne, c->d.elem_color,
                     c->d.N, c->d.dN, c->d.L, c->d.dL, c->d.gp, c->d.Gloc, c->d.edge_node, c->d.edge_dir,
                     c->d.rowptr, c->d.col, c->d.grow, c->d.gcol, c->d.gval, c->d.gtrow, c->d.gtcol, c->d.gtval,

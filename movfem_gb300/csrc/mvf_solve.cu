@@ -787,6 +787,7 @@ struct Work {
     double2 *pinvs = nullptr;  // vertex-patch inverses, one set per frequency
     double2 *xbest = nullptr;  // iterate with the lowest true residual so far
     float4 *xf = nullptr;      // float-float copy of the SpMM input (float-float operator)
+    MgWork *mg = nullptr;      // multilevel preconditioner of the 36/54-DOF systems
     int npol = 2, nfi = 1;
     // captured blocks of Arnoldi steps (see fgmres_cycle)
     static constexpr int GCH = 10, MAXB = 8;
@@ -805,6 +806,7 @@ static void free_work(Ctx *c, Work &W) {
     for (void *q : p)
         if (q) cudaFreeAsync(q, c->stream);
     if (W.pinvs) cudaFree(W.pinvs);
+    if (W.mg) mg_free(c, W.mg);
     W = Work{};
 }
 
@@ -1008,6 +1010,12 @@ static int cgs2(Ctx *c, Work &W, int k) {
 template <class TV>
 static void precondition(Ctx *c, Work &W, const TV *r, TV *z) {
     const int R = W.R;
+    if constexpr (std::is_same<TV, double2>::value) {
+        if (W.mg) {
+            mg_apply(c, W.mg, r, z);
+            return;
+        }
+    }
     if (W.pinvs) {
         patch_apply(c, W.pinvs, R, W.npol, W.nfi, r, z);
         return;
@@ -1154,7 +1162,11 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         std::vector<double> wl(nfs);
         for (int f = 0; f < nfs; ++f)
             wl[f] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f0 + f] : c->omega[f0 + f];
-        if ((rc = patch_invert(c, S, wl.data(), nfs, &W.pinvs))) { free_work(c, W); return rc; }
+        if (c->precond == 0)
+            rc = mg_numeric(c, S, wl.data(), nfs, R, npol, &W.mg);
+        else
+            rc = patch_invert(c, S, wl.data(), nfs, &W.pinvs);
+        if (rc) { free_work(c, W); return rc; }
         if (std::is_same<T, double>::value && c->solve_mode == 0 && c->patch_precision == 2 && R <= 8) {
             MVF_CUDA(c, cudaMallocAsync((void **)&W.xf, (size_t)W.n * R * sizeof(float4), c->stream));
             if ((rc = ensure_split(c, const_cast<MatrixSet &>(S)))) { free_work(c, W); return rc; }

@@ -75,6 +75,8 @@ def lib():
             L.orc_node_fields.argtypes = [P, P, I32, D, P, P, P, P, P, P]
             L.orc_check_sharing.restype = D
             L.orc_check_sharing.argtypes = [P]
+            L.orc_set_pmass.restype = None
+            L.orc_set_pmass.argtypes = [ctypes.c_int, D]
             L.orc_map_model.restype = ctypes.c_int
             L.orc_map_model.argtypes = [P, P, D, P, P]
             _lib = L

@@ -15,6 +15,35 @@
 
 typedef double complex cplx;
 
+/* Not the reference: the mass rule of the GPU library's multilevel preconditioner
+ * (mvf_mg.cu), switched on by orc_set_pmass for tests of that preconditioner.  The real
+ * part of the interpolated conductivity tensor at a Gauss point is shifted by twice the
+ * negative part of its Gershgorin lower bound (|sigma| for an isotropic tensor) plus a
+ * floor conductivity. */
+static int g_pmass_on = 0;
+static double g_pmass_floor = 0.0;
+
+void orc_set_pmass(int on, double floor_s) {
+    g_pmass_on = on;
+    g_pmass_floor = floor_s;
+}
+
+static const int PK6[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+
+static void pmass_sigma(cplx *mf2) {
+    double gmin = 1e300, shift;
+    int a, b;
+    for (a = 0; a < 3; a++) {
+        double off = 0.0, v;
+        for (b = 0; b < 3; b++)
+            if (b != a) off += fabs(creal(mf2[PK6[a][b]]));
+        v = creal(mf2[PK6[a][a]]) - off;
+        if (v < gmin) gmin = v;
+    }
+    shift = 2.0 * (gmin < 0.0 ? -gmin : 0.0) + g_pmass_floor;
+    for (a = 0; a < 3; a++) mf2[PK6[a][a]] += shift;
+}
+
 static const double PI = 3.1415926535897932384626433;      /* geometry.f90:25 */
 static const double EPS0 = 8.854187817e-12;                 /* geometry.f90:25 */
 static const double B0_PRIMARY = 1.0e-9;                     /* problem.f90:27 */
@@ -760,6 +789,7 @@ static int element_work(const orc_mesh *m, const elem_tab *t, const elem_geo *g,
                 w->mf2[gq][c] += Nn[i] * (sg[2 * c] + I * sg[2 * c + 1]);
             }
         }
+        if (g_pmass_on) pmass_sigma(w->mf2[gq]);
         if (!m->dirichlet) {
             double r[3] = {0, 0, 0};
             for (j = 0; j < t->mn; j++)

@@ -127,6 +127,11 @@ int orc_map_model(const orc_mesh *m, const orc_model *md, double omega, double *
  * tangential component of shared edge basis functions between face neighbours. */
 double orc_check_sharing(const orc_mesh *m);
 
+/* Test switch, not the reference: assemble the multilevel preconditioner's mass
+ * (interpolated conductivity shifted positive semidefinite, plus floor_s S/m) instead
+ * of the reference's. */
+void orc_set_pmass(int on, double floor_s);
+
 #ifdef __cplusplus
 }
 #endif

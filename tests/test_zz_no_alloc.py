@@ -1,18 +1,19 @@
 """mvf_spmv_noalloc: the matrix-vector product for callers that cannot let the
-library allocate device memory (their device memory belongs to their own pool, or
-the call sits between captured / latency-critical stream steps).
+library allocate device memory (their device memory belongs to their own pool
+allocator).
 
-It must give the same product as mvf_spmv (the allocating entry point) within the
-tolerance of the SpMV parity test, on two calls in a row -- the second call reuses
-the shared fixed-size staging array left behind by the first.  This file is
-collected last so that a failure here leaves the rest of the suite already run; it
-also passes on its own in a fresh process.
+It must give the same product as mvf_spmv (the allocating entry point) and as the
+oracle's assembled matrix, on two calls in a row -- the second call reuses the shared
+fixed-size staging array left behind by the first -- and it must leave the device's
+free memory unchanged.  This file is collected last so that a failure here leaves the
+rest of the suite already run; it also passes on its own in a fresh process.
 """
 import math
 
 import numpy as np
 import pytest
 
+import oracle
 from movfem_gb300 import api
 from movfem_gb300 import mesh as M
 
@@ -29,16 +30,24 @@ def test_noalloc_spmv_matches_spmv_twice():
     w = 2 * math.pi * np.array([0.5, 4.0])
     p = api.MTProblem(m, device=0)
     p.assemble(w)
+    o = oracle.Oracle(m)
     rng = np.random.Generator(np.random.PCG64(11))
     for call, f in enumerate([1, 0]):
         x = rng.normal(size=(2, p.nne)) + 1j * rng.normal(size=(2, p.nne))
         ref = p.spmv(f, x)
+        A, _ = o.matrix(w[f])
+        ref_oracle = np.stack([A @ x[0], A @ x[1]])
         xd = torch.from_numpy(x).to("cuda:0")
         yd = torch.full((2, p.nne), complex(float("nan"), float("nan")), dtype=torch.complex128, device="cuda:0")
         torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(0)[0]
         p.spmv_noalloc(f, xd.data_ptr(), yd.data_ptr())
+        free1 = torch.cuda.mem_get_info(0)[0]
         y = yd.cpu().numpy()
+        assert free1 == free0, f"call {call}: device free memory changed by {free0 - free1} bytes"
         assert _rel(y, ref) < 1e-12, f"call {call}"
+        # the oracle's matrix: FP64 on both sides, assembled in a different order
+        assert _rel(y, ref_oracle) < 1e-10, f"call {call}"
 
 
 def test_noalloc_rejects_models_above_its_limit():
