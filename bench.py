@@ -51,11 +51,15 @@ def make_config(name: str):
         return m, {"workload": "quadratic-40x40x30+8pml+10air-gpml-fang-8f", "elements": "quadratic-36-edge",
                    "cells": [56, 56, 56], "freqs": 8, "boundary": "gpml-fang"}
     if name == "quadratic-40x40x30-dirichlet":
+        # the headline model with the reference's Dirichlet boundary (boundary=1,
+        # inimod=1) on the same padded mesh and 8 frequencies log-spaced 0.1..100 Hz:
+        # below ~0.1 Hz two FP64 direct solves of this discretisation already differ in
+        # Z by more than the 1e-6 gate (tests/test_conditioning.py)
         m = M.layered_blocks(20261203, nodes_per_elem=20, ncx=40, ncy=40, ncz=30, d=50.0, nextd=8, n_air=10,
-                             dz_air=100.0, nfreq=8, fmin=1e-3, fmax=100.0, nrx=11, gpml_sch=0)
+                             dz_air=100.0, nfreq=8, fmin=0.1, fmax=100.0, nrx=11, gpml_sch=0)
         m.dirichlet = 1
-        return m, {"workload": "quadratic-40x40x30+8pad+10air-dirichlet-8f", "elements": "quadratic-36-edge",
-                   "cells": [56, 56, 56], "freqs": 8, "boundary": "dirichlet"}
+        return m, {"workload": "quadratic-40x40x30+8pad+10air-dirichlet-8f-0.1..100Hz", "elements": "quadratic-36-edge",
+                   "cells": [56, 56, 56], "freqs": 8, "band_hz": [0.1, 100.0], "boundary": "dirichlet"}
     raise SystemExit(f"unknown config {name}")
 
 
@@ -148,7 +152,7 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     m, cfg = make_config(args.config)
     if args.max_iters is None:
-        args.max_iters = 3000 if m.nodes_per_elem == 8 else 200
+        args.max_iters = 3000 if m.nodes_per_elem == 8 else 120
     cfg["max_iters"] = args.max_iters
     omega = 2 * math.pi * m.freqs
     sig_f = np.stack([m.sigma_at(w) for w in omega])
@@ -195,10 +199,12 @@ def run_ours(args):
             st_e, Z_e = step(True)
         torch.cuda.synchronize()
         e2e_s = time.time() - t1
-    zerr = float(np.max(np.linalg.norm(Z - Zref, axis=2) / np.linalg.norm(Zref, axis=2)))
+    zf = np.max(np.linalg.norm(Z - Zref, axis=2) / np.linalg.norm(Zref, axis=2), axis=1)  # per frequency
+    zerr = float(zf.max())
+    met = bool(zerr <= 1e-6)
     solves = nf * args.steps
-    value, dev_s = replica_aggregate(dist, dev_s, solves, device=f"cuda:{dev}")
-    e2e_value, e2e_s = replica_aggregate(dist, e2e_s, solves, device=f"cuda:{dev}")
+    rate, dev_s = replica_aggregate(dist, dev_s, solves, device=f"cuda:{dev}")
+    e2e_rate, e2e_s = replica_aggregate(dist, e2e_s, solves, device=f"cuda:{dev}")
     if rank != 0:
         return
     hbm, peak_kind = peaks()
@@ -211,38 +217,50 @@ def run_ours(args):
                  "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
                  "bytes_per_launch": spmm_bytes, "us_per_launch": prof["seconds_per_launch"] * 1e6, "traffic": None}
     roof = spmm_roof
+    dtype = "c64 Krylov in c128 refinement"
     if m.nodes_per_elem != 8:
-        # the 36/54-DOF solve runs in FP64 and its dominant kernel is the vertex-patch
-        # preconditioner (launch lists in profiles/): one application streams every
-        # patch inverse once
-        pp = prob.profile_patch(0, reps=5)
-        arith = {1: "FP64", 2: "float-float on the FP32 pipe"}.get(prob.patch_arithmetic(), "none")
-        pa = pp["bytes_per_apply"] / pp["seconds_per_apply"] / 1e9
-        kern = "patch_apply_ff_kernel" if prob.patch_arithmetic() == 2 else "patch_apply_kernel"
-        roof = {"bound": "hbm", "kernel": f"{kern}<double2> (8 colour launches; {arith})", "achieved": pa,
-                "peak": hbm, "unit": "GB/s", "frac": pa / hbm, "peak_kind": peak_kind,
-                "bytes_per_launch": pp["bytes_per_apply"], "us_per_launch": pp["seconds_per_apply"] * 1e6,
-                "traffic": None, "spmm_fp32": spmm_roof}
+        # the 36/54-DOF solve: FP64 Krylov vectors, float-float operator and level-0
+        # smoother, FP64 true residual; the dominant kernel is the level-0 smoothing
+        # sweep of the multilevel preconditioner (launch list in profiles/)
+        dtype = "c128 Krylov, float-float (FP32 pipe) operator and level-0 smoother, c128 true residual"
+        pm = prob.profile_mg(reps=3)
+        pa = pm["bytes_per_sweep"] / pm["seconds_per_sweep"] / 1e9
+        roof = {"bound": "hbm", "kernel": "mg_smooth_ff (one level-0 sweep: 8 colour launches, all frequencies)",
+                "achieved": pa, "peak": hbm, "unit": "GB/s", "frac": pa / hbm, "peak_kind": peak_kind,
+                "bytes_per_launch": pm["bytes_per_sweep"], "us_per_launch": pm["seconds_per_sweep"] * 1e6,
+                "traffic": TRAFFIC.get(args.config), "spmm_fp32": spmm_roof}
     line = {
-        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": rate if met else None, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_s / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "replicas", "vs_baseline": None, "dtype": "complex64-in-complex128-refinement",
+        "scaling": "replicas", "vs_baseline": None, "dtype": dtype,
         "data": "synthetic seeded model (numpy PCG64) of the named shape",
         "config": dict(cfg, l2="inputs larger than L2" if prob.nnz * 12 > 130e6 else "L2-resident",
-                       nne=prob.nne, nnz=prob.nnz, setup_s=round(setup_s, 3)),
-        "accuracy": {"max_rel_dZ_vs_fp64": zerr, "tolerance": 1e-6, "met": zerr <= 1e-6,
+                       nne=prob.nne, nnz=prob.nnz, setup_s=round(setup_s, 3),
+                       mg_levels=prob.mg_levels() if m.nodes_per_elem != 8 else None),
+        "accuracy": {"max_rel_dZ_vs_fp64": zerr, "rel_dZ_per_freq": [float(v) for v in zf], "tolerance": 1e-6,
+                     "met": met, "freqs_met": int((zf <= 1e-6).sum()), "rate_if_unmet": None if met else rate,
                      "rel_residual": st["rel_residual"], "inner_iters": st["inner_iters"],
                      "converged": st.get("converged"),
                      "fp64_rel_residual": st64["rel_residual"], "fp64_iters": st64["inner_iters"],
                      "fp64_plain_solves_per_s": nf / fp64_s if fp64_s > 0 else None},
-        "e2e": {"value": e2e_value, "unit": "solves/s",
+        "e2e": {"value": e2e_rate if met else None, "unit": "solves/s", "rate_if_unmet": None if met else e2e_rate,
                 "h2d_bytes_per_step": int(rhs.nbytes), "d2h_bytes_per_step": int(rhs.nbytes)},
         "roofline": roof,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if not met:
+        line["value_note"] = ("value is null: the mixed solve did not reach |dZ|/|Z| <= 1e-6 against the FP64 solve "
+                              "at every frequency within the iteration cap; rate_if_unmet gives the rate of the "
+                              "capped solve")
     line["cpu_baseline"] = cpu_baseline(args, m, omega, sig_f) if (not args.no_cpu and world == 1) else None
     print(json.dumps(line))
+
+
+# DRAM bytes (read + write) of one level-0 smoothing sweep, from an ncu capture of the
+# smaller model of the same kind scaled to the full model by its patch-inverse bytes
+# (profiles/mg_smooth_ff-quadratic.md); None until captured
+TRAFFIC = {}
 
 
 def cpu_baseline(args, m, omega, sig_f, budget_s=20.0):
@@ -274,8 +292,22 @@ def cpu_baseline(args, m, omega, sig_f, budget_s=20.0):
         if time.time() - t0 > budget_s or n >= 3:
             break
     dt = time.time() - t0
-    return {"value": n / dt, "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": f"{sample}; {n} solve(s) of {o.nne} DOF in {dt:.1f}s"}
+    out = {"value": n / dt, "unit": "solves/s", "cores": cores, "kind": "port",
+           "sample": f"{sample}; {n} solve(s) of {o.nne} DOF in {dt:.1f}s"}
+    if mm is not m:
+        # a 3-D nested-dissection direct factorisation costs ~ n^2 flops: the full model's
+        # rate, extrapolated from the sample, labelled as such
+        nfull = full_dofs(m)
+        out["extrapolated_full_model"] = {"value": (n / dt) * (o.nne / nfull) ** 2, "unit": "solves/s",
+                                          "dofs": nfull, "rule": "sample rate x (sample DOFs / full DOFs)^2",
+                                          "kind": "extrapolation"}
+    return out
+
+
+def full_dofs(m):
+    """Free DOFs of m (the oracle's numbering, without assembling)."""
+    import oracle
+    return int(oracle.Oracle(m).numbering()[1])
 
 
 BATCH = "batched-64-uneven"
@@ -445,11 +477,23 @@ def run_batched(args):
 
 
 def run_reference(args):
+    """The reference's CPU path on this arm's config: the C restatement of its assembly
+    plus SuperLU standing in for MUMPS (the Fortran program and MUMPS cannot be built
+    on either machine).  A model too large for that direct solve within a bounded run
+    prints an ``unavailable`` line; the GPU arm's ``cpu_baseline`` then carries a
+    measured scaled sample and its labelled extrapolation."""
     m, cfg = make_config(args.config)
     omega = 2 * math.pi * m.freqs
     sig_f = np.stack([m.sigma_at(w) for w in omega])
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if m.npt > 60000:
+        print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable": (
+            "the reference (Fortran + MUMPS 4.10) cannot be built here or on the GPU box, and its stand-in (C "
+            "restatement + SuperLU direct solve) on this %d-DOF quadratic system would take hours and far more "
+            "host memory than a bounded run allows (fill grows like n^(4/3), flops like n^2); the GPU arm's "
+            "cpu_baseline gives a measured scaled sample and its labelled extrapolation" % full_dofs(m))}))
         return
     vals = []
     for _ in range(args.warmup + args.steps):
@@ -469,13 +513,13 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="quadratic-40x40x30-gpml")
+    ap.add_argument("--config", default="quadratic-40x40x30-dirichlet")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--ref-tol", type=float, default=1e-12)
     ap.add_argument("--max-iters", type=int, default=None,
-                    help="Krylov iteration cap (default: 3000 for linear elements, 200 otherwise, so that a "
-                         "default run of the quadratic GPML workload ends within minutes)")
+                    help="Krylov iteration cap (default: 3000 for linear elements, 120 otherwise, so that a "
+                         "default run of the quadratic workload ends within minutes)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--threads", type=int, default=8, help="models in flight for the batched workload")
     args = ap.parse_args()

@@ -143,16 +143,28 @@ int mvf_set_solver(mvf_ctx *ctx, int32_t restart, int32_t mixed_passes, int32_t 
  * 36/54-DOF level, Galerkin coarsening to the 12-edge space on the same cells, then to
  * merged cells, down to a directly solved level.  It works on K + i w Mp, where Mp is
  * the mass matrix of the interpolated conductivity shifted positive semidefinite at
- * every Gauss point plus a floor conductivity (S/m; default 1e-8, <= 0 keeps the
- * setting) that makes the air's gradients regular.  kind 1: the one-level
+ * every Gauss point (the quadratic interpolation undershoots below zero next to
+ * jumps), plus a floor conductivity (S/m; default 1e-8, <= 0 keeps the setting) that
+ * makes the air's gradients regular, plus tau diag(K) (default 0, < 0 keeps the
+ * setting).  kind 2: the same without the semidefinite shift.  kind 1: the one-level
  * vertex-patch method.  Takes effect at the next mvf_assemble. */
-int mvf_set_preconditioner(mvf_ctx *ctx, int32_t kind, double tau);
+int mvf_set_preconditioner(mvf_ctx *ctx, int32_t kind, double floor_s, double tau);
 /* Levels of the multilevel preconditioner (0 when not in use) and the free DOFs of the
  * first cap of them (level 0 is the system itself). */
 int mvf_mg_levels(const mvf_ctx *ctx, int32_t *nlevels, int32_t *ndofs, int32_t cap);
 /* Test hook: one cycle of the multilevel preconditioner for frequency f applied to R
  * host right-hand sides r [n][R] complex; z [n][R] complex. */
 int mvf_mg_apply_once(mvf_ctx *ctx, int32_t f, int32_t R, const double *r, double *z);
+/* Measurement hook: one level-0 smoothing sweep of the multilevel preconditioner over
+ * every assembled frequency and both polarisations (mixed-mode arithmetic), timed on
+ * the library's stream; bytes: its algorithmic bytes (patch inverses, patch rows of
+ * the CSR, the patch DOFs' vectors). */
+int mvf_profile_mg(mvf_ctx *ctx, int32_t reps, double *sec_per_sweep, int64_t *bytes);
+/* Batching of the mixed mode (no counterpart in the reference): per_frequency 0 solves
+ * every frequency of a matrix set and both polarisations as one batch of right-hand
+ * sides (default), 1 solves one frequency (2 right-hand sides) per batch, so that each
+ * frequency stops at its own iteration count. */
+int mvf_set_batching(mvf_ctx *ctx, int32_t per_frequency);
 /* Arithmetic the last vertex-patch inversion set up: 0 no patches (12-DOF elements),
  * 1 FP64, 2 float-float (scaled inverses split into FP32 halves). */
 int32_t mvf_patch_arithmetic(const mvf_ctx *ctx);
@@ -207,7 +219,7 @@ const char *mvf_spmm_tuning(mvf_ctx *ctx);
 /* Parity hook for the autotuner's candidates (no reference counterpart): y = A_f x
  * for R right-hand sides (R a power of two <= 32) with SpMM variant `variant`
  * (0 chunked, 1 direct [R <= 4], 2..5 G = 4/8/16/32 lanes per row [R <= 16],
- * 6 float-float operator of the FP64 Krylov path [fp64 = 1, R <= 8]) in FP64
+ * 6 float-float operator of the FP64 Krylov path [fp64 = 1]) in FP64
  * (fp64 = 1: K, M and vectors FP64) or FP32 (K, M, vectors complex64); w is the
  * frequency's omega, rounded to FP32 when the mesh's quirks carry MVF_Q_FP32_CONST,
  * as in assembly.  x, y: host [nne][R] complex. */
@@ -218,8 +230,10 @@ int mvf_spmm_variant(mvf_ctx *ctx, int32_t f, int32_t variant, int32_t fp64, int
  * memory (a host whose device memory is owned by its own pool allocator, where a
  * cudaMalloc inside the library would fail or fragment that pool).  No counterpart in
  * the reference.  x, y: DEVICE pointers, [2][nne] complex.  Nothing is allocated: the
- * staging lives in a fixed 16 MiB device array shared by all calls, so nne must be
- * <= 262144 (MVF_E_ARG otherwise) and calls that overlap on the GPU race on it.  The
+ * staging lives in a fixed 16 MiB device array shared by all calls (part of the
+ * library's device image: with CUDA's lazy module loading it becomes resident when the
+ * first call loads that code on a device), so nne must be <= 262144 (MVF_E_ARG
+ * otherwise) and calls that overlap on the GPU race on it.  The
  * kernels run on the library's stream: x must be complete before the call (synchronise
  * the stream that wrote it); the call synchronises that stream and returns with y
  * complete.  The first call on a device looks up the array's device address and keeps

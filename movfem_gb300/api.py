@@ -58,7 +58,7 @@ EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numb
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
            "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many", "mvf_profile_patch",
-           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model", "mvf_set_preconditioner", "mvf_mg_levels", "mvf_mg_apply_once"]
+           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model", "mvf_set_preconditioner", "mvf_mg_levels", "mvf_mg_apply_once", "mvf_profile_mg", "mvf_set_batching"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
                "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params", "mvf_patch_arithmetic")
 SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
@@ -111,9 +111,11 @@ def load(build: bool = True):
     L.mvf_solve_many.argtypes = [P, I32, D, I32, I32, P, I32]
     L.mvf_profile_patch.argtypes = [P, I32, I32, P, P]
     L.mvf_set_solver.argtypes = [P, I32, I32, I32]
-    L.mvf_set_preconditioner.argtypes = [P, I32, ctypes.c_double]
+    L.mvf_set_preconditioner.argtypes = [P, I32, ctypes.c_double, ctypes.c_double]
     L.mvf_mg_levels.argtypes = [P, P, P, I32]
     L.mvf_mg_apply_once.argtypes = [P, I32, I32, P, P]
+    L.mvf_profile_mg.argtypes = [P, I32, P, P]
+    L.mvf_set_batching.argtypes = [P, I32]
     L.mvf_patch_arithmetic.argtypes = [P]
     L.mvf_patch_arithmetic.restype = I32
     L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
@@ -322,11 +324,15 @@ class MTProblem:
         preconditioner's arithmetic (1 FP64, 2 float-float); 0 keeps a setting."""
         self._chk(self.L.mvf_set_solver(self.h, restart, mixed_passes, patch_precision))
 
-    def set_preconditioner(self, kind: int = 0, tau: float = 0.0):
+    def set_preconditioner(self, kind: int = 0, floor: float = 0.0, tau: float = -1.0):
         """36/54-DOF preconditioner: 0 multilevel (default), 1 one-level vertex patches;
-        tau > 0 sets the multilevel operator's floor conductivity (S/m).  Call before
-        :meth:`assemble`."""
-        self._chk(self.L.mvf_set_preconditioner(self.h, kind, tau))
+        floor > 0 sets the multilevel operator's floor conductivity (S/m), tau >= 0 its
+        shift tau diag(K).  Call before :meth:`assemble`."""
+        self._chk(self.L.mvf_set_preconditioner(self.h, kind, floor, tau))
+
+    def set_batching(self, per_frequency: bool):
+        """Mixed mode: one batch per frequency (True) or all frequencies at once (False)."""
+        self._chk(self.L.mvf_set_batching(self.h, int(per_frequency)))
 
     def mg_levels(self):
         """Free DOFs of each level of the multilevel preconditioner (empty if unused)."""
@@ -341,6 +347,13 @@ class MTProblem:
         z = np.empty_like(r2)
         self._chk(self.L.mvf_mg_apply_once(self.h, f, r2.shape[1], _p(r2), _p(z)))
         return z.reshape(np.asarray(r).shape)
+
+    def profile_mg(self, reps: int = 3):
+        """Seconds and algorithmic bytes of one level-0 smoothing sweep (all frequencies)."""
+        s = ctypes.c_double()
+        b = ctypes.c_int64()
+        self._chk(self.L.mvf_profile_mg(self.h, reps, ctypes.byref(s), ctypes.byref(b)))
+        return {"seconds_per_sweep": s.value, "bytes_per_sweep": b.value}
 
     def patch_arithmetic(self) -> int:
         """0 no patches, 1 FP64, 2 float-float (as set up by the last inversion)."""

@@ -49,6 +49,8 @@ struct AsmParams {
     int64_t nb;
     const int32_t *bidx;
     const double2 *bep;
+    double mg_tau;  // shift tau diag(K_e) of the multilevel preconditioner's mass
+    int mg_abs;     // shift the preconditioner's conductivity positive semidefinite
 };
 
 __constant__ AsmParams c_ap;
@@ -314,7 +316,7 @@ __global__ void __launch_bounds__(256) element_kernel(
                             if (b != a) off += fabs(mf2[pk(a, b)].re);
                         gmin = fmin(gmin, mf2[pk(a, a)].re - off);
                     }
-                    const double shift = 2.0 * fmax(0.0, -gmin) + sfloor;
+                    const double shift = (c_ap.mg_abs ? 2.0 * fmax(0.0, -gmin) : 0.0) + sfloor;
                     for (int a = 0; a < 3; ++a)
                         for (int b = 0; b < 3; ++b)
                             S.dmp[gl][a][b] = w * (cmul(H, mf2[pk(a, b)]).re + (a == b ? H.re * shift : 0.0));
@@ -625,6 +627,10 @@ __global__ void __launch_bounds__(256) element_kernel(
                     }
                 }
                 __syncthreads();
+                // optional shift tau diag(K_e) of the preconditioner's mass
+                if (c_ap.mg_tau > 0.0)
+                    for (int i = tid; i < ME; i += blockDim.x) Ms[i * ME + i] += c_ap.mg_tau * Ks[i * ME + i];
+                __syncthreads();
                 for (int t = tid; t < 144; t += blockDim.x) {
                     const int a = t / 12, b = t % 12;
                     double k = 0.0, mm = 0.0;
@@ -708,6 +714,8 @@ static void set_params(Ctx *c, AsmParams &ap, int fset, int nfb, const double *o
     ap.lift = dirichlet_lift(*c) ? 1 : 0;
     ap.q9 = (m.quirks & MVF_Q_LIN_DZETA) ? 1 : 0;
     ap.nb = (int64_t)c->bnode_h.size();
+    ap.mg_tau = c->mg_tau;
+    ap.mg_abs = c->mg_abs;
     ap.bidx = c->d.bidx;
     ap.bep = c->d.bep;
     (void)fset;

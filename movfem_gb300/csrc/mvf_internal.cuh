@@ -21,6 +21,24 @@
 
 namespace mvf {
 
+#ifdef __CUDACC__
+// s += a*b with a, b float-float, as a compensated dot product (Ogita, Rump and Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005, Dot2): the high part
+// by TwoSum, every rounding error (the product's by FMA, the cross terms, the sum's)
+// collected in a plain FP32 low part without renormalising at each step.  The high
+// part's dependency chain is one addition per product.
+__device__ __forceinline__ void dot2_mac(float &sh, float &sl, float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, fmaf(al, bh, e));
+    const float t = sh + p;
+    const float bb = t - sh;
+    const float err = (sh - (t - bb)) + (p - bb);
+    sh = t;
+    sl += e + err;
+}
+#endif
+
 // Element-order constants and tables evaluated at the Gauss points.
 struct OrderTables {
     int mn = 0, me = 0, nord = 0, ngp = 0;
@@ -175,6 +193,9 @@ struct Ctx {
     // (S/m) of its operator
     int precond = 0;
     double mg_floor = 1e-8;
+    double mg_tau = 0.0;  // optional shift tau diag(K) of the preconditioner's mass
+    int mg_abs = 1;       // shift the preconditioner's conductivity positive semidefinite
+    int freq_batch = 0;  // mixed mode: 0 every frequency of a matrix set in one batch, 1 one per batch
     std::vector<MgLevel> mg;
 };
 

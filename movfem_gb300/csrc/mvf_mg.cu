@@ -157,6 +157,172 @@ __global__ void __launch_bounds__(128) mg_smooth(int64_t p0, int64_t p1, const i
     }
 }
 
+// The same colour sweep in float-float arithmetic on the FP32 pipe (the mixed mode's
+// level 0, where the FP64 version is bound by GB300's FP64 rate): K, Mp, the inverses,
+// the right-hand side and the iterate all held as hi + lo FP32 pairs, every row sum and
+// every inverse row a compensated dot product (dot2_mac), every update a float-float
+// addition -- about twice FP32's precision, with no FP64 instruction in the sweep.
+struct ffv {
+    float h, l;
+};
+__device__ __forceinline__ ffv ff_norm(float s, float e) {
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+__device__ __forceinline__ ffv ff_add(ffv a, ffv b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb) + a.l + b.l;
+    return ff_norm(s, e);
+}
+__device__ __forceinline__ ffv ff_mul(ffv a, ffv b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ void split_d(double v, float &h, float &l) {
+    h = __double2float_rn(v);
+    l = __double2float_rn(v - (double)h);
+}
+
+// row g of b - (K + i w Mp) x for right-hand side q, float-float: (re, im)
+__device__ __forceinline__ void ff_row(int32_t g, int q, int R, const int64_t *__restrict__ rowptr,
+                                       const int32_t *__restrict__ col, const float2 *__restrict__ K,
+                                       const float2 *__restrict__ M, ffv w, float4 bv, const float4 *__restrict__ x,
+                                       ffv &rr, ffv &ri) {
+    float krh = 0.f, krl = 0.f, kih = 0.f, kil = 0.f, mrh = 0.f, mrl = 0.f, mih = 0.f, mil = 0.f;
+    for (int64_t k = rowptr[g]; k < rowptr[g + 1]; ++k) {
+        const float2 kv = K[k], mv = M[k];
+        const float4 xv = x[(int64_t)col[k] * R + q];  // (re_hi, im_hi, re_lo, im_lo)
+        dot2_mac(krh, krl, kv.x, kv.y, xv.x, xv.z);
+        dot2_mac(kih, kil, kv.x, kv.y, xv.y, xv.w);
+        dot2_mac(mrh, mrl, mv.x, mv.y, xv.x, xv.z);
+        dot2_mac(mih, mil, mv.x, mv.y, xv.y, xv.w);
+    }
+    const ffv kr = ff_norm(krh, krl), ki = ff_norm(kih, kil), mr = ff_norm(mrh, mrl), mi = ff_norm(mih, mil);
+    const ffv wmi = ff_mul(w, mi), wmr = ff_mul(w, mr);
+    // b - (Kx_re - w Mx_im), b - (Kx_im + w Mx_re)
+    rr = ff_add(ff_add({bv.x, bv.z}, {-kr.h, -kr.l}), wmi);
+    ri = ff_add(ff_add({bv.y, bv.w}, {-ki.h, -ki.l}), {-wmr.h, -wmr.l});
+}
+
+__global__ void __launch_bounds__(128) mg_smooth_ff(int64_t p0, int64_t p1, const int64_t *__restrict__ pptr,
+                                                    const int32_t *__restrict__ pdof, const int64_t *__restrict__ ioff,
+                                                    const float4 *__restrict__ inv, int64_t fstride,
+                                                    const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+                                                    const float2 *__restrict__ K, const float2 *__restrict__ M,
+                                                    const float2 *__restrict__ wq, int R, int npol, int nfi,
+                                                    const float4 *__restrict__ b, float4 *__restrict__ x) {
+    extern __shared__ float4 rsf[];  // [P][R]: (re_hi, im_hi, re_lo, im_lo)
+    for (int64_t p = p0 + blockIdx.x; p < p1; p += gridDim.x) {
+        const int64_t b0 = pptr[p];
+        const int P = (int)(pptr[p + 1] - b0);
+        for (int t = threadIdx.x; t < P * R; t += blockDim.x) {
+            const int i = t / R, q = t % R;
+            const int32_t g = pdof[b0 + i];
+            const float2 w2 = wq[q];
+            ffv rr, ri;
+            ff_row(g, q, R, rowptr, col, K, M, {w2.x, w2.y}, b[(int64_t)g * R + q], x, rr, ri);
+            rsf[t] = make_float4(rr.h, ri.h, rr.l, ri.l);
+        }
+        __syncthreads();
+        const float4 *A = inv + ioff[p];
+        for (int t = threadIdx.x; t < P * R; t += blockDim.x) {
+            const int i = t / R, q = t % R;
+            const float4 *Ai = A + (int64_t)min(q / npol, nfi - 1) * fstride + (int64_t)i * P;
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+            for (int j = 0; j < P; ++j) {
+                const float4 a = Ai[j];
+                const float4 v = rsf[j * R + q];
+                dot2_mac(rh, rl, a.x, a.z, v.x, v.z);
+                dot2_mac(rh, rl, -a.y, -a.w, v.y, v.w);
+                dot2_mac(ih, il, a.x, a.z, v.y, v.w);
+                dot2_mac(ih, il, a.y, a.w, v.x, v.z);
+            }
+            float4 &o = x[(int64_t)pdof[b0 + i] * R + q];
+            const ffv zr = ff_add({o.x, o.z}, ff_norm(rh, rl)), zi = ff_add({o.y, o.w}, ff_norm(ih, il));
+            o = make_float4(zr.h, zi.h, zr.l, zi.l);
+        }
+        __syncthreads();
+    }
+}
+
+// t = b - A x over all rows (level 0 of the mixed mode), FP64 out
+__global__ void mg_resid_ff(int32_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+                            const float2 *__restrict__ K, const float2 *__restrict__ M, const float2 *__restrict__ wq,
+                            int R, const float4 *__restrict__ b, const float4 *__restrict__ x,
+                            double2 *__restrict__ t) {
+    const int64_t nt = (int64_t)n * R;
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nt; u += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t g = (int32_t)(u / R);
+        const int q = (int)(u % R);
+        const float2 w2 = wq[q];
+        ffv rr, ri;
+        ff_row(g, q, R, rowptr, col, K, M, {w2.x, w2.y}, b[u], x, rr, ri);
+        t[u] = make_double2((double)rr.h + (double)rr.l, (double)ri.h + (double)ri.l);
+    }
+}
+
+// float-float copies of complex FP64 vectors and back
+__global__ void mg_to_ff(int64_t n, const double2 *__restrict__ a, float4 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = a[i];
+        float rh, rl, ih, il;
+        split_d(v.x, rh, rl);
+        split_d(v.y, ih, il);
+        out[i] = make_float4(rh, ih, rl, il);
+    }
+}
+__global__ void mg_from_ff(int64_t n, const float4 *__restrict__ a, double2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = a[i];
+        out[i] = make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
+    }
+}
+
+// x (float-float) += S y for a real sparse S (the prolongation into level 0)
+__global__ void mg_prolong_ff(int32_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+                              const double *__restrict__ val, int R, const double2 *__restrict__ y,
+                              float4 *__restrict__ x) {
+    const int64_t nt = (int64_t)n * R;
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nt; u += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t g = (int32_t)(u / R);
+        const int q = (int)(u % R);
+        double sr = 0.0, si = 0.0;
+        for (int64_t k = rowptr[g]; k < rowptr[g + 1]; ++k) {
+            const double2 v = y[(int64_t)col[k] * R + q];
+            sr += val[k] * v.x;
+            si += val[k] * v.y;
+        }
+        const float4 o = x[u];
+        float h, l;
+        split_d(sr, h, l);
+        const ffv zr = ff_add({o.x, o.z}, {h, l});
+        split_d(si, h, l);
+        const ffv zi = ff_add({o.y, o.w}, {h, l});
+        x[u] = make_float4(zr.h, zi.h, zr.l, zi.l);
+    }
+}
+
+// FP64 values as hi + lo FP32 halves; inverses in place (double2 -> float4, same bytes)
+__global__ void mg_split(int64_t n, const double *__restrict__ a, float2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float h, l;
+        split_d(a[i], h, l);
+        out[i] = make_float2(h, l);
+    }
+}
+__global__ void mg_split_inv(int64_t n, double2 *__restrict__ a) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = a[i];
+        float rh, rl, ih, il;
+        split_d(v.x, rh, rl);
+        split_d(v.y, ih, il);
+        reinterpret_cast<float4 *>(a)[i] = make_float4(rh, ih, rl, il);
+    }
+}
+
 // t = b - A x over all rows of a level
 __global__ void mg_resid(int32_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
                          const double *__restrict__ K, const double *__restrict__ M, double tau,
@@ -529,6 +695,10 @@ struct MgWork {
     std::vector<double2 *> inv;          // per level, [nf][patch entries]
     std::vector<double2 *> b, x, t;      // per level, [n][R] (level 0: b, x are the caller's)
     double *wq = nullptr;                // [R] angular frequency of each right-hand side
+    bool ff = false;                     // level 0 in float-float (mixed mode)
+    float2 *Kff = nullptr, *Mff = nullptr;  // level-0 K and Mp as FP32 halves
+    float2 *wff = nullptr;                  // [R] angular frequencies as FP32 halves
+    float4 *bff = nullptr, *xff = nullptr;  // level-0 right-hand side and iterate, [n][R]
 };
 
 // patch-inverse workspace rows of one level: blocks x pmax x 2 pmax complex
@@ -555,6 +725,11 @@ void mg_free(Ctx *c, MgWork *W) {
         p.push_back(W->t[l]);
     }
     p.push_back(W->wq);
+    p.push_back(W->Kff);
+    p.push_back(W->Mff);
+    p.push_back(W->wff);
+    p.push_back(W->bff);
+    p.push_back(W->xff);
     for (void *q : p)
         if (q) cudaFree(q);
     delete W;
@@ -641,11 +816,36 @@ int mg_numeric(Ctx *c, const MatrixSet &S, const double *w, int nf, int R, int n
         }
     }
     MG_CUDA(cudaGetLastError());
+    // the mixed mode sweeps level 0 in float-float: K, Mp and the inverses split
+    W->ff = c->solve_mode == 0;
+    if (W->ff) {
+        MG_CUDA(cudaMalloc((void **)&W->Kff, c->nnz * sizeof(float2)));
+        MG_CUDA(cudaMalloc((void **)&W->Mff, c->nnz * sizeof(float2)));
+        count_launch();
+        mg_split<<<grid_n(c->nnz), 256, 0, c->stream>>>(c->nnz, S.K64, W->Kff);
+        count_launch();
+        mg_split<<<grid_n(c->nnz), 256, 0, c->stream>>>(c->nnz, S.Mp64, W->Mff);
+        count_launch();
+        mg_split_inv<<<grid_n(c->patch_entries * nf), 256, 0, c->stream>>>(c->patch_entries * nf, W->inv[0]);
+        MG_CUDA(cudaGetLastError());
+        MG_CUDA(cudaFuncSetAttribute(mg_smooth_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+    }
     // angular frequency per right-hand side, as the inverses were formed
     std::vector<double> wq(R);
     for (int q = 0; q < R; ++q) wq[q] = w[std::min(q / npol, nf - 1)];
     MG_CUDA(cudaMalloc((void **)&W->wq, R * sizeof(double)));
     MG_CUDA(cudaMemcpyAsync(W->wq, wq.data(), R * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (W->ff) {
+        std::vector<float2> wf(R);
+        for (int q = 0; q < R; ++q) {
+            const float h = (float)wq[q];
+            wf[q] = make_float2(h, (float)(wq[q] - (double)h));
+        }
+        MG_CUDA(cudaMalloc((void **)&W->wff, R * sizeof(float2)));
+        MG_CUDA(cudaMemcpyAsync(W->wff, wf.data(), R * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+        MG_CUDA(cudaMalloc((void **)&W->bff, (size_t)c->nne * R * sizeof(float4)));
+        MG_CUDA(cudaMalloc((void **)&W->xff, (size_t)c->nne * R * sizeof(float4)));
+    }
     int herr = 0;
     MG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     MG_CUDA(cudaStreamSynchronize(c->stream));
@@ -680,25 +880,56 @@ static void vcycle(Ctx *c, MgWork *W, int l) {
     const int64_t ent = fine ? c->patch_entries : c->mg[l - 1].pent;
     const int pmax = fine ? c->patch_max : c->mg[l - 1].pmax;
     const size_t sm = (size_t)pmax * R * sizeof(double2);
-    cudaMemsetAsync(W->x[l], 0, (size_t)n * R * sizeof(double2), c->stream);
+    const bool ff = fine && W->ff;
+    if (ff) {
+        count_launch();
+        mg_to_ff<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>((int64_t)n * R, W->b[l], W->bff);
+        cudaMemsetAsync(W->xff, 0, (size_t)n * R * sizeof(float4), c->stream);
+    } else {
+        cudaMemsetAsync(W->x[l], 0, (size_t)n * R * sizeof(double2), c->stream);
+    }
     auto sweep = [&](int col8) {
         const int64_t a = pco[col8], b = pco[col8 + 1];
         if (b <= a) return;
         count_launch();
-        mg_smooth<<<(unsigned)std::min<int64_t>(b - a, 152 * 16), 128, sm, c->stream>>>(
-            a, b, pptr, pdof, pioff, W->inv[l], ent, rowptr, col, K, M, tau, W->wq, R, W->npol, W->nf, W->b[l], W->x[l]);
+        const unsigned grid = (unsigned)std::min<int64_t>(b - a, 152 * 16);
+        if (ff)
+            mg_smooth_ff<<<grid, 128, (size_t)pmax * R * sizeof(float4), c->stream>>>(
+                a, b, pptr, pdof, pioff, reinterpret_cast<const float4 *>(W->inv[l]), ent, rowptr, col, W->Kff, W->Mff,
+                W->wff, R, W->npol, W->nf, W->bff, W->xff);
+        else
+            mg_smooth<<<grid, 128, sm, c->stream>>>(a, b, pptr, pdof, pioff, W->inv[l], ent, rowptr, col, K, M, tau,
+                                                    W->wq, R, W->npol, W->nf, W->b[l], W->x[l]);
     };
     for (int col8 = 0; col8 < 8; ++col8) sweep(col8);
-    if (l == nl - 1) return;  // the coarsest level: one patch, solved exactly
+    if (l == nl - 1) {  // the coarsest level: one patch, solved exactly
+        if (ff) {
+            count_launch();
+            mg_from_ff<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>((int64_t)n * R, W->xff, W->x[l]);
+        }
+        return;
+    }
     const MgLevel &C = c->mg[l];  // the next coarser level
     count_launch();
-    mg_resid<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>(n, rowptr, col, K, M, tau, W->wq, R, W->b[l], W->x[l], W->t[l]);
+    if (ff)
+        mg_resid_ff<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>(n, rowptr, col, W->Kff, W->Mff, W->wff, R, W->bff,
+                                                                  W->xff, W->t[l]);
+    else
+        mg_resid<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>(n, rowptr, col, K, M, tau, W->wq, R, W->b[l], W->x[l],
+                                                               W->t[l]);
     count_launch();
     mg_spmv<<<grid_n((int64_t)C.n * R), 256, 0, c->stream>>>(C.n, C.ptrow, C.ptcol, C.ptval, R, W->t[l], W->b[l + 1], 0);
     vcycle(c, W, l + 1);
     count_launch();
-    mg_spmv<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>(n, C.prow, C.pcol, C.pval, R, W->x[l + 1], W->x[l], 1);
+    if (ff)
+        mg_prolong_ff<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>(n, C.prow, C.pcol, C.pval, R, W->x[l + 1], W->xff);
+    else
+        mg_spmv<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>(n, C.prow, C.pcol, C.pval, R, W->x[l + 1], W->x[l], 1);
     for (int col8 = 7; col8 >= 0; --col8) sweep(col8);
+    if (ff) {
+        count_launch();
+        mg_from_ff<<<grid_n((int64_t)n * R), 256, 0, c->stream>>>((int64_t)n * R, W->xff, W->x[l]);
+    }
 }
 
 void mg_apply(Ctx *c, MgWork *W, const double2 *r, double2 *z) {
@@ -713,10 +944,14 @@ void mg_apply(Ctx *c, MgWork *W, const double2 *r, double2 *z) {
 
 using namespace mvf;
 
-extern "C" int mvf_set_preconditioner(mvf_ctx *xc, int32_t kind, double tau) {
-    if (!xc || kind < 0 || kind > 1) return MVF_E_ARG;
+extern "C" int mvf_set_preconditioner(mvf_ctx *xc, int32_t kind, double floor_s, double tau) {
+    if (!xc || kind < 0 || kind > 2) return MVF_E_ARG;
     Ctx *c = &xc->c;
-    if (tau > 0.0) c->mg_floor = tau;
+    // kind 2: the multilevel method on the true conductivity (no semidefinite shift)
+    c->mg_abs = kind == 2 ? 0 : 1;
+    if (kind == 2) kind = 0;
+    if (floor_s > 0.0) c->mg_floor = floor_s;
+    if (tau >= 0.0) c->mg_tau = tau;
     c->precond = kind;
     if (kind == 0 && c->use_patches && c->mg.empty()) return mg_setup(c);
     return 0;
@@ -745,7 +980,12 @@ extern "C" int mvf_mg_apply_once(mvf_ctx *xc, int32_t f, int32_t R, const double
         if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
     const double w = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
     MgWork *W = nullptr;
-    if (int rc = mg_numeric(c, *S, &w, 1, R, R, &W)) return rc;
+    // FP64 throughout, the arithmetic of the plain mode
+    const int mode = c->solve_mode;
+    c->solve_mode = 1;
+    const int rc0 = mg_numeric(c, *S, &w, 1, R, R, &W);
+    c->solve_mode = mode;
+    if (rc0) return rc0;
     const size_t vb = (size_t)c->nne * R * sizeof(double2);
     double2 *dr = nullptr, *dz = nullptr;
     cudaError_t e = cudaMalloc((void **)&dr, vb);
@@ -761,5 +1001,79 @@ extern "C" int mvf_mg_apply_once(mvf_ctx *xc, int32_t f, int32_t R, const double
     cudaFree(dz);
     mg_free(c, W);
     if (e != cudaSuccess) return cuda_fail(c, e, "multilevel apply");
+    return 0;
+}
+
+// Measurement hook: one level-0 smoothing sweep (8 colour launches) of the multilevel
+// preconditioner over every assembled frequency and both polarisations, in the mixed
+// mode's arithmetic, timed with CUDA events on the library's stream.  Algorithmic bytes
+// per sweep: every patch inverse of every frequency (16 B an entry), the CSR rows of
+// the patch DOFs (column index, K and Mp halves: 20 B a nonzero) and the patch DOFs'
+// right-hand side read, iterate read and write (16 B each per right-hand side).
+extern "C" int mvf_profile_mg(mvf_ctx *xc, int32_t reps, double *sec_per_sweep, int64_t *bytes) {
+    if (!xc || !sec_per_sweep || reps < 1) return MVF_E_ARG;
+    Ctx *c = &xc->c;
+    if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
+    if (!c->use_patches || c->precond != 0) return fail(c, MVF_E_UNSUPPORTED, "multilevel preconditioner not in use");
+    const MatrixSet &S = c->sets[0];
+    const int nf = S.nfreq, npol = 2;
+    int R = 1;
+    while (R < nf * npol) R <<= 1;
+    std::vector<double> w(nf);
+    for (int f = 0; f < nf; ++f)
+        w[f] = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[S.first_freq + f] : c->omega[S.first_freq + f];
+    const int mode = c->solve_mode;
+    c->solve_mode = 0;
+    MgWork *W = nullptr;
+    const int rc0 = mg_numeric(c, S, w.data(), nf, R, npol, &W);
+    c->solve_mode = mode;
+    if (rc0) return rc0;
+    const size_t vb = (size_t)c->nne * R * sizeof(double2);
+    double2 *b = nullptr, *x = nullptr;
+    cudaError_t e = cudaMalloc((void **)&b, vb);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&x, vb);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b, 0, vb, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(x, 0, vb, c->stream);
+    float ms = 0.f;
+    if (e == cudaSuccess) {
+        auto sweep = [&]() {
+            for (int col8 = 0; col8 < 8; ++col8) {
+                const int64_t a = c->pcolor_off[col8], bb = c->pcolor_off[col8 + 1];
+                if (bb <= a) continue;
+                count_launch();
+                mg_smooth_ff<<<(unsigned)std::min<int64_t>(bb - a, 152 * 16), 128,
+                               (size_t)c->patch_max * R * sizeof(float4), c->stream>>>(
+                    a, bb, c->d.patch_ptr, c->d.patch_dof, c->d.patch_ioff, reinterpret_cast<const float4 *>(W->inv[0]),
+                    c->patch_entries, c->d.rowptr, c->d.col, W->Kff, W->Mff, W->wff, R, npol, nf,
+                    reinterpret_cast<const float4 *>(b), reinterpret_cast<float4 *>(x));
+            }
+        };
+        sweep();
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, c->stream);
+        for (int i = 0; i < reps; ++i) sweep();
+        cudaEventRecord(e1, c->stream);
+        e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    cudaFree(b);
+    cudaFree(x);
+    mg_free(c, W);
+    if (e != cudaSuccess) return cuda_fail(c, e, "multilevel profile");
+    *sec_per_sweep = ms * 1e-3 / reps;
+    if (bytes) {
+        // rows of the patch DOFs, counted on the host from the pattern
+        std::vector<int64_t> rp(c->nne + 1), pp(c->npatch + 1);
+        std::vector<int32_t> pd(c->patch_dofs);
+        cudaMemcpy(rp.data(), c->d.rowptr, rp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost);
+        cudaMemcpy(pd.data(), c->d.patch_dof, pd.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        int64_t rows = 0;
+        for (int32_t g : pd) rows += rp[g + 1] - rp[g];
+        *bytes = (int64_t)nf * c->patch_entries * 16 + rows * 20 + c->patch_dofs * (int64_t)(nf * npol) * 16 * 3;
+    }
     return 0;
 }

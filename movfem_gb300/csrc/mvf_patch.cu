@@ -269,22 +269,6 @@ __global__ void __launch_bounds__(128) patch_apply_kernel(int64_t p0, int64_t p1
 // precision, against 24 bits for plain FP32 -- enough for inverses whose air-gradient
 // components dwarf the rest.
 
-// s += a*b with a, b float-float, as a compensated dot product (Ogita, Rump and Oishi,
-// "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005, Dot2): the high part
-// by TwoSum, every rounding error (the product's by FMA, the cross terms, the sum's)
-// collected in a plain FP32 low part without renormalising at each step.  The high
-// part's dependency chain is one addition per product.
-__device__ __forceinline__ void dot2_mac(float &sh, float &sl, float ah, float al, float bh, float bl) {
-    const float p = ah * bh;
-    float e = fmaf(ah, bh, -p);
-    e = fmaf(ah, bl, fmaf(al, bh, e));
-    const float t = sh + p;
-    const float bb = t - sh;
-    const float err = (sh - (t - bb)) + (p - bb);
-    sh = t;
-    sl += e + err;
-}
-
 // The inverses span many orders of magnitude (air patches, PML stretch), beyond what
 // FP32 halves can hold.  Each patch's inverse is therefore stored scaled symmetrically,
 // S = D^-1 A_v^-1 D^-1 with d_i = sqrt|A_v^-1_ii| (1 where that vanishes), and the

@@ -308,13 +308,15 @@ __global__ void split_vector(int64_t n, const double2 *__restrict__ x, float4 *_
     }
 }
 
-// y = (K + i w M) x for R right-hand sides, G lanes per row, each lane all R; the
-// group's float-float partial sums meet by xor-shuffles with TwoSum.
+// y = (K + i w M) x for R right-hand sides r0 .. r0+R-1 of vectors holding RS per row,
+// G lanes per row, each lane all R; the group's float-float partial sums meet by
+// xor-shuffles with TwoSum.
 template <int R, int G>
 __global__ void __launch_bounds__(256) spmm_ff(int32_t n, const int64_t *__restrict__ rowptr,
                                                const int32_t *__restrict__ col, const float2 *__restrict__ K,
                                                const float2 *__restrict__ M, const float4 *__restrict__ x,
-                                               double2 *__restrict__ y, const SolveParams *__restrict__ sp) {
+                                               double2 *__restrict__ y, const SolveParams *__restrict__ sp, int RS,
+                                               int r0) {
     constexpr int RPW = 32 / G;
     const int lane = threadIdx.x & 31, g = lane / G, j = lane % G;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -337,7 +339,7 @@ __global__ void __launch_bounds__(256) spmm_ff(int32_t n, const int64_t *__restr
             const float2 kv = __ldg(K + k), mv = __ldg(M + k);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const float4 xv = __ldg(x + (int64_t)c * R + r);
+                const float4 xv = __ldg(x + (int64_t)c * RS + r0 + r);
                 ffm(acc[r][0], acc[r][1], kv.x, kv.y, xv.x, xv.z);
                 ffm(acc[r][2], acc[r][3], kv.x, kv.y, xv.y, xv.w);
                 ffm(acc[r][4], acc[r][5], mv.x, mv.y, xv.x, xv.z);
@@ -358,10 +360,10 @@ __global__ void __launch_bounds__(256) spmm_ff(int32_t n, const int64_t *__restr
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 if (r % G != j) continue;
-                const double w = sp->w32[r];
+                const double w = sp->w32[r0 + r];
                 const double kr = (double)acc[r][0] + acc[r][1], ki = (double)acc[r][2] + acc[r][3];
                 const double mr = (double)acc[r][4] + acc[r][5], mi = (double)acc[r][6] + acc[r][7];
-                y[row * R + r] = make_double2(kr - w * mi, ki + w * mr);
+                y[row * RS + r0 + r] = make_double2(kr - w * mi, ki + w * mr);
             }
         }
     }
@@ -608,11 +610,12 @@ __global__ void scale_into(int32_t n, int R, const TV *__restrict__ w, const dou
 
 // Hessenberg column k for each rhs: h[0..k] from the two CGS passes (hc), h[k+1] =
 // ||w||; apply the previous Givens rotations, form the new one, update g.
+constexpr int MAXM = 256;  // longest FGMRES cycle (restart length)
 struct Hess {
-    double2 H[64][65];  // H[row][col], (m+1) x m
-    double2 cs[64];     // cos (real) packed in .x; sin complex
-    double2 sn[64];
-    double2 g[65];
+    double2 H[MAXM][MAXM + 1];  // H[row][col], (m+1) x m
+    double2 cs[MAXM];           // cos (real) packed in .x; sin complex
+    double2 sn[MAXM];
+    double2 g[MAXM + 1];
     double beta;
     int active;
 };
@@ -621,41 +624,27 @@ struct Hess {
 // updates: it is held in shared memory (one column per right-hand side, lane r) so
 // the chain waits on shared-memory latency, and the rotations are read up front.
 __global__ void hessenberg_step(int R, int k, const double2 *__restrict__ hc, const double2 *__restrict__ wn2, Hess *hs) {
-    constexpr int RC = 16;  // rotations staged per chunk (static shared memory < 48 KB)
-    __shared__ double2 col[65][32];
-    __shared__ double2 sn_s[RC][32];
-    __shared__ double cs_s[RC][32];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R || threadIdx.x >= 32 || k > 63) return;
+    if (r >= R || k >= MAXM) return;
     Hess &S = hs[r];
-    const int l = threadIdx.x;
-    for (int i = 0; i <= k; ++i) col[i][l] = hc[i * R + r];
-    col[k + 1][l] = make_double2(sqrt(fmax(wn2[r].x, 0.0)), 0.0);
-    // previous rotations: [c s; -conj(s) c] with c real
+    // previous rotations [c s; -conj(s) c] (c real) applied down the new column: rotation
+    // i mixes entries i and i+1; entry i is then final, entry i+1 carries on.  The loads
+    // of hc and the rotations do not depend on the chain, which is arithmetic only.
+    double2 carry = hc[r];
     for (int i = 0; i < k; ++i) {
-        if (i % RC == 0) {
-            // stage the next RC rotations (independent loads, all in flight at once)
-#pragma unroll
-            for (int q = 0; q < RC; ++q)
-                if (i + q < k) {
-                    cs_s[q][l] = S.cs[i + q].x;
-                    sn_s[q][l] = S.sn[i + q];
-                }
-        }
-        const double c = cs_s[i % RC][l];
-        const double2 s = sn_s[i % RC][l];
-        const double2 a = col[i][l], b = col[i + 1][l];
+        const double c = S.cs[i].x;
+        const double2 s = S.sn[i];
+        const double2 a = carry, b = hc[(i + 1) * R + r];
         double2 t1, t2;
         t1.x = c * a.x + (s.x * b.x - s.y * b.y);
         t1.y = c * a.y + (s.x * b.y + s.y * b.x);
         t2.x = -(s.x * a.x + s.y * a.y) + c * b.x;
         t2.y = -(s.x * a.y - s.y * a.x) + c * b.y;
-        col[i][l] = t1;
-        col[i + 1][l] = t2;
+        S.H[i][k] = t1;
+        carry = t2;
     }
-    for (int i = 0; i < k; ++i) S.H[i][k] = col[i][l];
-    const double2 a = col[k][l];
-    const double bb = col[k + 1][l].x;  // real and >= 0
+    const double2 a = carry;
+    const double bb = sqrt(fmax(wn2[r].x, 0.0));  // ||w||, real and >= 0
     const double na = hypot(a.x, a.y);
     double c;
     double2 s;
@@ -678,13 +667,21 @@ __global__ void hessenberg_step(int R, int k, const double2 *__restrict__ hc, co
     S.g[k + 1] = make_double2(-(s.x * gk.x + s.y * gk.y), -(s.x * gk.y - s.y * gk.x));
 }
 
+// residual estimate |g[k]| / beta of every right-hand side after k steps
+__global__ void hessenberg_est(int R, int k, const Hess *hs, double *__restrict__ est) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const Hess &S = hs[r];
+    est[r] = S.beta > 0 ? hypot(S.g[k].x, S.g[k].y) / S.beta : 0.0;
+}
+
 __global__ void hessenberg_init(int R, const double2 *__restrict__ rn2, Hess *hs) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= R) return;
     const double b = sqrt(fmax(rn2[r].x, 0.0));
     hs[r].beta = b;
     hs[r].g[0] = make_double2(b, 0.0);
-    for (int i = 1; i < 65; ++i) hs[r].g[i] = make_double2(0.0, 0.0);
+    for (int i = 1; i < MAXM + 1; ++i) hs[r].g[i] = make_double2(0.0, 0.0);
 }
 
 // back substitution: y = H(0:k,0:k)^-1 g(0:k), stored in yout[j][r].  One warp per
@@ -692,9 +689,9 @@ __global__ void hessenberg_init(int R, const double2 *__restrict__ rn2, Hess *hs
 // y_j (j = lane, lane + 32) and a shuffle sum, so the row chain waits on one
 // reduction instead of k dependent loads.
 __global__ void hessenberg_solve(int R, int k, Hess *hs, double2 *__restrict__ yout) {
-    __shared__ double2 y[64];
+    __shared__ double2 y[MAXM];
     const int r = blockIdx.x, lane = threadIdx.x;
-    if (r >= R || k > 64) return;
+    if (r >= R || k > MAXM) return;
     Hess &S = hs[r];
     for (int i = k - 1; i >= 0; --i) {
         double tr = 0.0, ti = 0.0;
@@ -783,6 +780,7 @@ struct Work {
     double2 *partial = nullptr, *hc = nullptr, *htmp = nullptr, *nrm = nullptr, *y = nullptr;
     double *kd = nullptr, *md = nullptr;
     Hess *hs = nullptr;
+    double *est = nullptr;  // [R] residual estimates of the running cycle
     size_t vb = 0;
     double2 *pinvs = nullptr;  // vertex-patch inverses, one set per frequency
     double2 *xbest = nullptr;  // iterate with the lowest true residual so far
@@ -802,7 +800,7 @@ static void free_work(Ctx *c, Work &W) {
     for (cudaGraphExec_t &g : W.blocks)
         if (g) cudaGraphExecDestroy(g);
     void *p[] = {W.V, W.Z, W.w, W.t, W.x64, W.b64, W.r64, W.dinv, W.pinv, W.partial, W.hc, W.htmp, W.nrm, W.y, W.kd, W.md, W.hs,
-                 W.xbest, W.xf};
+                 W.xbest, W.xf, W.est};
     for (void *q : p)
         if (q) cudaFreeAsync(q, c->stream);
     if (W.pinvs) cudaFree(W.pinvs);
@@ -839,6 +837,10 @@ static int alloc_work(Ctx *c, Work &W, int R, int m) {
     MVF_CUDA(c, cudaMallocAsync((void **)&W.kd, (size_t)W.n * sizeof(double), c->stream));
     MVF_CUDA(c, cudaMallocAsync((void **)&W.md, (size_t)W.n * sizeof(double), c->stream));
     MVF_CUDA(c, cudaMallocAsync((void **)&W.hs, (size_t)R * sizeof(Hess), c->stream));
+    MVF_CUDA(c, cudaMallocAsync((void **)&W.est, (size_t)R * sizeof(double), c->stream));
+    // the projections of a long cycle need more than the default 48 KB of shared memory
+    MVF_CUDA(c, cudaFuncSetAttribute(multidot<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)std::max<size_t>(48 * 1024, (size_t)(m + 1) * R * sizeof(double2))));
     return 0;
 }
 
@@ -957,10 +959,16 @@ static void launch_spmm_ff(Ctx *c, const MatrixSet &S, int R, const double2 *x, 
     const SolveParams *sp = (const SolveParams *)c->d.wsp;
     count_launch();
     switch (R) {
-        case 1: spmm_ff<1, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp); break;
-        case 2: spmm_ff<2, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp); break;
-        case 4: spmm_ff<4, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp); break;
-        default: spmm_ff<8, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp); break;
+        case 1: spmm_ff<1, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp, 1, 0); break;
+        case 2: spmm_ff<2, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp, 2, 0); break;
+        case 4: spmm_ff<4, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp, 4, 0); break;
+        default:
+            // R = 8, 16, 32: passes of 8 right-hand sides
+            for (int r0 = 0; r0 < R; r0 += 8) {
+                if (r0) count_launch();
+                spmm_ff<8, G><<<grid, 256, 0, c->stream>>>(c->nne, c->d.rowptr, c->d.col, S.Kff, S.Mff, xf, y, sp, R, r0);
+            }
+            break;
     }
 }
 
@@ -1050,7 +1058,6 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
     hessenberg_init<<<1, 32, 0, c->stream>>>(R, W.nrm, W.hs);
     count_launch();
     scale_into<TV><<<grid_for(vs), 256, 0, c->stream>>>(W.n, R, w, W.nrm, V);
-    std::vector<Hess> hh(R);
     // one Arnoldi step: z_k = P v_k, w = A z_k, orthogonalise, v_{k+1} = w / ||w||
     auto step = [&](int k) -> int {
         precondition<TV>(c, W, V + k * vs, Z + k * vs);
@@ -1105,14 +1112,13 @@ static int fgmres_cycle(Ctx *c, Work &W, const MatrixSet &S, const typename C2<T
                 if (int rc = step(kk)) return rc;
         k = k1;
         // residual estimate after the block
-        MVF_CUDA(c, cudaMemcpyAsync(hh.data(), W.hs, sizeof(Hess) * R, cudaMemcpyDeviceToHost, c->stream));
+        count_launch();
+        hessenberg_est<<<1, 32, 0, c->stream>>>(R, k, W.hs, W.est);
+        MVF_CUDA(c, cudaMemcpyAsync(est.data(), W.est, sizeof(double) * R, cudaMemcpyDeviceToHost, c->stream));
         MVF_CUDA(c, cudaStreamSynchronize(c->stream));
         bool all = true;
-        for (int r = 0; r < R; ++r) {
-            const double g = hypot(hh[r].g[k].x, hh[r].g[k].y);
-            est[r] = hh[r].beta > 0 ? g / hh[r].beta : 0.0;
+        for (int r = 0; r < R; ++r)
             if (est[r] > tol_abs_rel) all = false;
-        }
         if (all) break;
     }
     ++W.cycles;
@@ -1167,7 +1173,7 @@ static int solve_set(Ctx *c, const MatrixSet &S, int f0, int nfs, int pol0, int 
         else
             rc = patch_invert(c, S, wl.data(), nfs, &W.pinvs);
         if (rc) { free_work(c, W); return rc; }
-        if (std::is_same<T, double>::value && c->solve_mode == 0 && c->patch_precision == 2 && R <= 8) {
+        if (std::is_same<T, double>::value && c->solve_mode == 0 && c->patch_precision == 2) {
             MVF_CUDA(c, cudaMallocAsync((void **)&W.xf, (size_t)W.n * R * sizeof(float4), c->stream));
             if ((rc = ensure_split(c, const_cast<MatrixSet &>(S)))) { free_work(c, W); return rc; }
         }
@@ -1316,13 +1322,18 @@ extern "C" int mvf_solve(mvf_ctx *xc, double *rhs_inout, double tol, int32_t mod
     int rc = 0, noconv = 0;
     for (const MatrixSet &S : c->sets) {
         if (mode == 0) {
-            // all frequencies of the set and both polarisations in one batch; complex
-            // FP32 Krylov vectors, except with the vertex-patch preconditioner of the
-            // 36/54-DOF elements, whose air-patch inverses need FP64 vectors
-            int r = c->use_patches ? solve_set<double>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, c->restart)
-                                   : solve_set<float>(c, S, S.first_freq, S.nfreq, 0, 2, tol, max_iters, st, c->restart);
-            if (r == MVF_E_NOCONV) noconv = 1;
-            else if (r) { rc = r; break; }
+            // all frequencies of the set and both polarisations in one batch (or one
+            // frequency per batch); complex FP32 Krylov vectors, except with the
+            // preconditioners of the 36/54-DOF elements, which need FP64 vectors
+            const int step = c->freq_batch == 1 ? 1 : S.nfreq;
+            for (int f0 = S.first_freq; f0 < S.first_freq + S.nfreq && !rc; f0 += step) {
+                const int nfs = std::min(step, S.first_freq + S.nfreq - f0);
+                int r = c->use_patches ? solve_set<double>(c, S, f0, nfs, 0, 2, tol, max_iters, st, c->restart)
+                                       : solve_set<float>(c, S, f0, nfs, 0, 2, tol, max_iters, st, c->restart);
+                if (r == MVF_E_NOCONV) noconv = 1;
+                else if (r) rc = r;
+            }
+            if (rc) break;
         } else {
             for (int f = S.first_freq; f < S.first_freq + S.nfreq && !rc; ++f)
                 for (int p = 0; p < 2 && !rc; ++p) {
@@ -1386,7 +1397,7 @@ extern "C" int mvf_solve_many(mvf_ctx **ctx, int32_t n, double tol, int32_t mode
 extern "C" int mvf_set_solver(mvf_ctx *xc, int32_t restart, int32_t mixed_passes, int32_t patch_precision) {
     if (!xc) return MVF_E_ARG;
     Ctx *c = &xc->c;
-    if (restart != 0 && (restart < 2 || restart > 63)) return fail(c, MVF_E_ARG, "restart must be 2..63");
+    if (restart != 0 && (restart < 2 || restart > MAXM)) return fail(c, MVF_E_ARG, "restart must be 2..256");
     if (mixed_passes != 0 && (mixed_passes < 1 || mixed_passes > 2)) return fail(c, MVF_E_ARG, "passes must be 1 or 2");
     if (patch_precision != 0 && patch_precision != 1 && patch_precision != 2)
         return fail(c, MVF_E_ARG, "patch precision must be 1 (FP64) or 2 (float-float)");
@@ -1397,6 +1408,12 @@ extern "C" int mvf_set_solver(mvf_ctx *xc, int32_t restart, int32_t mixed_passes
 }
 
 extern "C" int64_t mvf_kernel_launches(void) { return launch_counter().load(); }
+
+extern "C" int mvf_set_batching(mvf_ctx *xc, int32_t per_frequency) {
+    if (!xc || per_frequency < 0 || per_frequency > 1) return MVF_E_ARG;
+    xc->c.freq_batch = per_frequency;
+    return 0;
+}
 
 extern "C" int mvf_set_guess(mvf_ctx *xc, const double *x0) {
     if (!xc) return MVF_E_ARG;
@@ -1428,9 +1445,9 @@ extern "C" int mvf_spmm_variant(mvf_ctx *xc, int32_t f, int32_t variant, int32_t
     Ctx *c = &xc->c;
     if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
     if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
-    const bool ffv = variant == SPMM_VARIANTS;  // the float-float operator (FP64 vectors, R <= 8)
+    const bool ffv = variant == SPMM_VARIANTS;  // the float-float operator (FP64 vectors)
     if (R < 1 || R > MAXR || (R & (R - 1)) || variant < 0 || variant > SPMM_VARIANTS ||
-        (!ffv && !spmm_ok(variant, R)) || (ffv && (!fp64 || R > 8)))
+        (!ffv && !spmm_ok(variant, R)) || (ffv && !fp64))
         return fail(c, MVF_E_ARG, "bad variant / right-hand-side count");
     const MatrixSet *S = nullptr;
     for (const MatrixSet &s : c->sets)

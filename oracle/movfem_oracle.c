@@ -18,8 +18,8 @@ typedef double complex cplx;
 /* Not the reference: the mass rule of the GPU library's multilevel preconditioner
  * (mvf_mg.cu), switched on by orc_set_pmass for tests of that preconditioner.  The real
  * part of the interpolated conductivity tensor at a Gauss point is shifted by twice the
- * negative part of its Gershgorin lower bound (|sigma| for an isotropic tensor) plus a
- * floor conductivity. */
+ * negative part of its Gershgorin lower bound (|sigma| for an isotropic tensor; on = 1
+ * only) plus a floor conductivity (on = 1 or 2). */
 static int g_pmass_on = 0;
 static double g_pmass_floor = 0.0;
 
@@ -40,7 +40,7 @@ static void pmass_sigma(cplx *mf2) {
         v = creal(mf2[PK6[a][a]]) - off;
         if (v < gmin) gmin = v;
     }
-    shift = 2.0 * (gmin < 0.0 ? -gmin : 0.0) + g_pmass_floor;
+    shift = (g_pmass_on == 1 ? 2.0 * (gmin < 0.0 ? -gmin : 0.0) : 0.0) + g_pmass_floor;
     for (a = 0; a < 3; a++) mf2[PK6[a][a]] += shift;
 }
 

@@ -128,8 +128,8 @@ int orc_map_model(const orc_mesh *m, const orc_model *md, double omega, double *
 double orc_check_sharing(const orc_mesh *m);
 
 /* Test switch, not the reference: assemble the multilevel preconditioner's mass
- * (interpolated conductivity shifted positive semidefinite, plus floor_s S/m) instead
- * of the reference's. */
+ * instead of the reference's: on = 1 the interpolated conductivity shifted positive
+ * semidefinite plus floor_s S/m, on = 2 plus floor_s only, on = 0 the reference's. */
 void orc_set_pmass(int on, double floor_s);
 
 #ifdef __cplusplus

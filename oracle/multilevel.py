@@ -6,8 +6,9 @@ scipy, the one the GPU library uses for its 36/54-DOF systems (``mvf_mg.cu``), s
 test can compare one preconditioner cycle computed both ways on the same input:
 
 * level 0: K + i w Mp, where Mp is the mass matrix of the interpolated conductivity
-  shifted positive semidefinite at every Gauss point plus a floor conductivity (the
-  oracle's ``orc_set_pmass`` switch); FGMRES keeps the true A = K + i w M;
+  shifted positive semidefinite at every Gauss point (optional) plus a floor
+  conductivity (the oracle's ``orc_set_pmass`` switch), plus tau diag(K) (optional);
+  FGMRES keeps the true A = K + i w M;
 * level 1: the 12-edge space on the same cells, prolongation from the exact local
   combination of the 36/54-DOF element's edge functions (:func:`p_local`), operator
   P^T A P;
@@ -231,17 +232,20 @@ class Multilevel:
     """The preconditioner of one frequency w (angular; FP32-rounded as the assembly
     does when the mesh keeps the FP32-constant quirk) for mesh m (20/27 nodes)."""
 
-    def __init__(self, m, omega, floor=1e-8):
+    def __init__(self, m, omega, floor=1e-8, tau=0.0, semidefinite=True):
         from . import lib
+        w = float(np.float32(omega)) if (m.quirks & 2) else float(omega)
         o = Oracle(m)
         o.set_sigma(m.sigma_at(omega))
         A, self.rhs = o.matrix(omega)
         self.A_true = A.tocsr()
-        lib().orc_set_pmass(1, float(floor))
+        lib().orc_set_pmass(1 if semidefinite else 2, float(floor))
         try:
             A0 = Oracle(m, sigma=m.sigma_at(omega)).matrix(omega)[0].tocsr()
         finally:
             lib().orc_set_pmass(0, 0.0)
+        if tau > 0:
+            A0 = (A0 + 1j * w * tau * sp.diags(self.A_true.real.diagonal())).tocsr()
         gq, nq = o.numbering()
         self.A = [A0]
         self.P = []
