@@ -53,3 +53,21 @@ def test_fang_b0_one_gives_no_reproducible_fp64_answer():
 def test_moderate_stretch_is_reproducible(gpml_sch, b0):
     for f in (1e-3, 1.0):
         assert _z_spread(_model(gpml_sch, b0, f), f) < 1e-6
+
+
+@pytest.mark.parametrize("f,bound", [(1.0, 1e-7), (100.0, 1e-7)])
+def test_quadratic_dirichlet_band_is_reproducible(f, bound):
+    """The headline band (1..100 Hz, quadratic elements, Dirichlet boundary): two FP64
+    direct solves agree in Z at least ten times below the 1e-6 gate."""
+    m = M.layered_blocks(7, nodes_per_elem=20, ncx=6, ncy=6, ncz=4, d=50.0, nextd=2, n_air=3, dz_air=100.0,
+                         nfreq=1, fmin=f, fmax=f, nrx=4, gpml_sch=0)
+    m.dirichlet = 1
+    assert _z_spread(m, f) < bound
+
+
+def test_quadratic_dirichlet_below_the_band_is_not_reproducible():
+    """At 1 mHz the same comparison differs by far more than the gate."""
+    m = M.layered_blocks(7, nodes_per_elem=20, ncx=6, ncy=6, ncz=4, d=50.0, nextd=2, n_air=3, dz_air=100.0,
+                         nfreq=1, fmin=1e-3, fmax=1e-3, nrx=4, gpml_sch=0)
+    m.dirichlet = 1
+    assert _z_spread(m, 1e-3) > 1e-5
