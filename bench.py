@@ -82,6 +82,8 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        if os.environ.get("MVF_BENCH_NO_CLOCKS"):
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -550,14 +552,18 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--ref-tol", type=float, default=1e-12)
-    ap.add_argument("--ref-iters", type=int, default=800,
+    ap.add_argument("--ref-iters", type=int, default=400,
                     help="iteration cap of the accuracy reference of the 36/54-DOF workloads")
     ap.add_argument("--max-iters", type=int, default=None,
                     help="Krylov iteration cap (default: 3000 for linear elements, 120 otherwise, so that a "
                          "default run of the quadratic workload ends within minutes)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-clocks", action="store_true",
+                    help="do not sample nvidia-smi (for runs under a profiler, which follows child processes)")
     ap.add_argument("--threads", type=int, default=8, help="models in flight for the batched workload")
     args = ap.parse_args()
+    if args.no_clocks:
+        os.environ["MVF_BENCH_NO_CLOCKS"] = "1"
     if args.config == MAP:
         if args.impl == "reference":
             m, gm, cfg = make_map_config()
