@@ -132,11 +132,12 @@ int mvf_element_matrices(const mvf_ctx *ctx, int64_t e0, int64_t count, int32_t 
 int mvf_solve(mvf_ctx *ctx, double *rhs_inout, double tol, int32_t mode, int32_t max_iters, mvf_stats *st);
 
 /* Solver settings of a context (no counterpart in the reference): FGMRES restart
- * length (2..63, default 30), Gram-Schmidt passes of the mixed mode (1 or 2,
- * default 1), and the arithmetic of the vertex-patch preconditioner of the 36/54-DOF
- * elements in the mixed mode: 1 FP64, 2 float-float on the FP32 pipe (default; falls
- * back to FP64 when a scaled inverse entry does not fit two FP32 halves).  The plain
- * FP64 mode always applies it in FP64.  0 keeps a setting. */
+ * length (2..256, default 30), Gram-Schmidt passes of the mixed mode (1 or 2,
+ * default 1), and the arithmetic of the one-level vertex-patch preconditioner of the
+ * 36/54-DOF elements (mvf_set_preconditioner kind 1) in the mixed mode: 1 FP64, 2
+ * float-float on the FP32 pipe (default; falls back to FP64 when a scaled inverse
+ * entry does not fit two FP32 halves).  The plain FP64 mode always applies it in FP64.
+ * 0 keeps a setting. */
 int mvf_set_solver(mvf_ctx *ctx, int32_t restart, int32_t mixed_passes, int32_t patch_precision);
 /* Preconditioner of the 36/54-DOF systems (no counterpart in the reference, which
  * factorises with MUMPS).  kind 0: multilevel (default): vertex-patch smoothing on the
