@@ -115,6 +115,12 @@ int mvf_assemble(mvf_ctx *ctx, int32_t nfreq, const double *omega, const double 
  * MUMPS (before ga_sort_sparse, exact zeros kept), 1-based, in row-major order.
  * ia/ja/a may be NULL to query *nnz.  a is complex. */
 int mvf_export_coo(const mvf_ctx *ctx, int32_t f, int32_t *ia, int32_t *ja, double *a, int64_t *nnz);
+/* The same COO with the exact-zero entries left out, as find_zeros / rem_zeros leave
+ * them out before the MUMPS call (global_assembly.f90:123-150, MoVFEM_3DMT.f90:85-97):
+ * *nnz = entries kept, *nzero = entries dropped (value exactly 0 + 0i).  ia/ja/a may be
+ * NULL to query both counts; the kept entries stay in the same order. */
+int mvf_export_coo_nz(const mvf_ctx *ctx, int32_t f, int32_t *ia, int32_t *ja, double *a, int64_t *nnz,
+                      int64_t *nzero);
 /* Right-hand sides of frequency f: [2][nne] complex (mumps_par%rhs layout). */
 int mvf_export_rhs(const mvf_ctx *ctx, int32_t f, double *rhs);
 
@@ -283,6 +289,51 @@ typedef struct mvf_model {
  * device; otherwise that device, and the caller's current device is restored. */
 int mvf_map_model(const mvf_mesh *grid, const mvf_model *model, double omega, double *sigma_out, double *mu_out,
                   double *seconds, int32_t device);
+
+/* ---- Gridding (the step before the model mapping) ---------------------------------
+ * grid_3d (geometry.f90:48-118) on the host: padding from the skin depth (extension),
+ * sub-layers between interfaces (zblocks), node coordinates (gauss_grid, local_gqg,
+ * complete_grid), the interfaces interpolated by the modified quadratic Shepard method
+ * of ACM TOMS 660 (toms660.f90).  Arguments as read_input leaves them
+ * (read_input.f90:47-162), in the input's coordinates. */
+typedef struct mvf_grid_in {
+    double dx, dy, dz;        /* core cell sizes (in_dx, in_dy, in_dz) */
+    double high, depth;       /* air above the highest / earth below the deepest interface point */
+    int32_t nodes_per_elem;   /* 8, 20 or 27 (in_mn) */
+    double sigma_bg;          /* conductivity of the skin-depth estimate (in_bcksigma) */
+    int32_t nsr;              /* receivers */
+    const double *rx;         /* [nsr][3] x, y, z */
+    int32_t nsf0;             /* input interfaces, top (earth surface) last */
+    const int32_t *nsp;       /* [nsf0] points per interface (>= 20 each) */
+    const double *pts;        /* [sum nsp][3] interface points, interface after interface */
+    int32_t mx, my, mz;       /* inner model grid */
+    const double *xm, *ym;    /* [mx], [my] */
+    const double *zm;         /* [mx*my*mz] */
+    int32_t nf;               /* frequencies (the lowest sets the padding) */
+    const double *freqs;      /* [nf] Hz */
+} mvf_grid_in;
+
+typedef struct mvf_grid_info {
+    int32_t nodes_per_elem;
+    int32_t nextd;            /* padding cells per side */
+    int32_t nsf;              /* interfaces incl. the three added ones (in_nsf) */
+    int32_t nx, ny, nz;       /* cells per axis (g_nx-1, g_ny-1, g_nz-1) */
+    int64_t nnx, nny, nnz, npt;
+    int32_t nzl_top, nzl_air; /* g_nzl(nsf), g_nzl(nsf-1) */
+    double x0, y0, z0;        /* shift of coord_transform: grid = input - (x0, y0, z0) */
+    double ztop;              /* g_ztop: lowest point of the top input interface, shifted */
+    double skin_depth, nd;    /* the padding's target: sum of padding widths > nd * skin_depth */
+} mvf_grid_info;
+
+typedef struct mvf_grid mvf_grid;
+/* Build the grid.  MVF_E_ARG for invalid input, including an interface with fewer than
+ * 20 points or one QSHEP2 cannot fit (the reference reads unset memory there); the
+ * message is mvf_last_error(NULL). */
+int mvf_grid_3d(const mvf_grid_in *in, mvf_grid **grid);
+int mvf_grid_get_info(const mvf_grid *grid, mvf_grid_info *info);
+/* g_xp [nnx], g_yp [nny], g_zp [npt] (node (i*nny + j)*nnz + k), g_nzl [nsf]; any may be NULL. */
+int mvf_grid_export(const mvf_grid *grid, double *xp, double *yp, double *zp, int32_t *nzl);
+void mvf_grid_destroy(mvf_grid *grid);
 
 /* ---- Learned warm start (no counterpart in the reference) -------------------------
  * A dilated 3-D convolutional operator on a cell grid: nconv 3x3x3 convolutions of

@@ -53,14 +53,16 @@ class Stats(ctypes.Structure):
 
 
 EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numbering", "mvf_set_sigma",
-           "mvf_assemble", "mvf_export_coo", "mvf_export_rhs", "mvf_element_matrices", "mvf_solve",
+           "mvf_assemble", "mvf_export_coo", "mvf_export_coo_nz", "mvf_export_rhs", "mvf_element_matrices", "mvf_solve",
            "mvf_impedance", "mvf_spmv", "mvf_profile_spmm", "mvf_kernel_launches", "mvf_spmv_noalloc",
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
            "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many", "mvf_profile_patch",
-           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model", "mvf_set_preconditioner", "mvf_mg_levels", "mvf_mg_apply_once", "mvf_profile_mg", "mvf_set_batching"]
+           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model", "mvf_set_preconditioner", "mvf_mg_levels", "mvf_mg_apply_once", "mvf_profile_mg", "mvf_set_batching",
+           "mvf_grid_3d", "mvf_grid_get_info", "mvf_grid_export", "mvf_grid_destroy"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
-               "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params", "mvf_patch_arithmetic")
+               "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params", "mvf_patch_arithmetic",
+               "mvf_grid_destroy")
 SPMM_VARIANTS = {0: "chunked", 1: "direct", 2: "vec/G=4", 3: "vec/G=8", 4: "vec/G=16", 5: "vec/G=32"}
 
 
@@ -96,6 +98,7 @@ def load(build: bool = True):
     L.mvf_set_sigma.argtypes = [P, P]
     L.mvf_assemble.argtypes = [P, I32, P, P, I32]
     L.mvf_export_coo.argtypes = [P, I32, P, P, P, P]
+    L.mvf_export_coo_nz.argtypes = [P, I32, P, P, P, P, P]
     L.mvf_export_rhs.argtypes = [P, I32, P]
     L.mvf_element_matrices.argtypes = [P, I64, I64, I32, P, P, P]
     L.mvf_solve.argtypes = [P, P, D, I32, I32, P]
@@ -133,6 +136,11 @@ def load(build: bool = True):
     L.mvf_spmm_tuning.argtypes = [P]
     L.mvf_spmm_tuning.restype = ctypes.c_char_p
     L.mvf_map_model.argtypes = [P, P, D, P, P, P, I32]
+    L.mvf_grid_3d.argtypes = [P, ctypes.POINTER(P)]
+    L.mvf_grid_get_info.argtypes = [P, P]
+    L.mvf_grid_export.argtypes = [P, P, P, P, P]
+    L.mvf_grid_destroy.argtypes = [P]
+    L.mvf_grid_destroy.restype = None
     for n in EXPORTS:
         if n not in _NOT_STATUS:
             getattr(L, n).restype = ctypes.c_int
@@ -142,6 +150,67 @@ def load(build: bool = True):
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+class _GridIn(ctypes.Structure):
+    _fields_ = [
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("high", ctypes.c_double),
+        ("depth", ctypes.c_double), ("nodes_per_elem", ctypes.c_int32), ("sigma_bg", ctypes.c_double),
+        ("nsr", ctypes.c_int32), ("rx", ctypes.c_void_p), ("nsf0", ctypes.c_int32), ("nsp", ctypes.c_void_p),
+        ("pts", ctypes.c_void_p), ("mx", ctypes.c_int32), ("my", ctypes.c_int32), ("mz", ctypes.c_int32),
+        ("xm", ctypes.c_void_p), ("ym", ctypes.c_void_p), ("zm", ctypes.c_void_p), ("nf", ctypes.c_int32),
+        ("freqs", ctypes.c_void_p),
+    ]
+
+
+class GridInfo(ctypes.Structure):
+    _fields_ = [
+        ("nodes_per_elem", ctypes.c_int32), ("nextd", ctypes.c_int32), ("nsf", ctypes.c_int32),
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("nnx", ctypes.c_int64),
+        ("nny", ctypes.c_int64), ("nnz", ctypes.c_int64), ("npt", ctypes.c_int64), ("nzl_top", ctypes.c_int32),
+        ("nzl_air", ctypes.c_int32), ("x0", ctypes.c_double), ("y0", ctypes.c_double), ("z0", ctypes.c_double),
+        ("ztop", ctypes.c_double), ("skin_depth", ctypes.c_double), ("nd", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def grid_3d(dx, dy, dz, high, depth, nodes_per_elem, sigma_bg, rx, interfaces, xm, ym, zm, freqs):
+    """Node grid of the model domain (``mvf_grid_3d``: grid_3d, geometry.f90:48-118, on
+    the host in native code).  ``rx`` [nsr, 3]; ``interfaces``: one [n, 3] array of
+    points per input interface, deepest first (read_top_interfaces order,
+    read_input.f90:72-101); ``xm`` [mx], ``ym`` [my], ``zm`` [mx, my, mz] the inner
+    model's coordinates; ``freqs`` in Hz.  Returns ``(info, xp, yp, zp, nzl)``: ``info``
+    a dict of :class:`GridInfo` (the grid coordinates are the input's minus
+    ``(x0, y0, z0)``), ``zp`` of node ``(i*nny + j)*nnz + k``."""
+    L = load()
+    rxa = np.ascontiguousarray(rx, dtype=np.float64).reshape(-1, 3)
+    ifs = [np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3) for p in interfaces]
+    nsp = np.array([p.shape[0] for p in ifs], dtype=np.int32)
+    pts = np.ascontiguousarray(np.concatenate(ifs, axis=0))
+    xma = np.ascontiguousarray(xm, dtype=np.float64)
+    yma = np.ascontiguousarray(ym, dtype=np.float64)
+    zma = np.ascontiguousarray(zm, dtype=np.float64)
+    fa = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
+    gi = _GridIn(float(dx), float(dy), float(dz), float(high), float(depth), int(nodes_per_elem), float(sigma_bg),
+                 rxa.shape[0], _p(rxa), len(ifs), _p(nsp), _p(pts), xma.size, yma.size, zma.size // (xma.size * yma.size),
+                 _p(xma), _p(yma), _p(zma), fa.size, _p(fa))
+    h = ctypes.c_void_p()
+    rc = L.mvf_grid_3d(ctypes.byref(gi), ctypes.byref(h))
+    if rc != 0:
+        raise MVFError(rc, L.mvf_last_error(None).decode())
+    try:
+        info = GridInfo()
+        L.mvf_grid_get_info(h, ctypes.byref(info))
+        xp = np.empty(info.nnx)
+        yp = np.empty(info.nny)
+        zp = np.empty(info.npt)
+        nzl = np.empty(info.nsf, dtype=np.int32)
+        L.mvf_grid_export(h, _p(xp), _p(yp), _p(zp), _p(nzl))
+    finally:
+        L.mvf_grid_destroy(h)
+    return info.as_dict(), xp, yp, zp, nzl
 
 
 class _Model(ctypes.Structure):
@@ -262,13 +331,23 @@ class MTProblem:
         self._chk(self.L.mvf_assemble(self.h, om.size, _p(om), _p(sf), ifreq0))
         self.omega = om
 
-    def export_coo(self, f: int = 0):
+    def export_coo(self, f: int = 0, drop_zeros: bool = False):
+        """Lower-triangle COO (1-based, row-major) of frequency ``f``.  ``drop_zeros``
+        leaves out the exact-zero entries as ``find_zeros``/``rem_zeros`` do
+        (global_assembly.f90:123-150) and records how many in ``self.zeros_dropped``."""
         n = ctypes.c_int64()
-        self._chk(self.L.mvf_export_coo(self.h, f, None, None, None, ctypes.byref(n)))
+        z = ctypes.c_int64()
+        if drop_zeros:
+            call = lambda *a: self.L.mvf_export_coo_nz(self.h, f, *a, ctypes.byref(n), ctypes.byref(z))
+        else:
+            call = lambda *a: self.L.mvf_export_coo(self.h, f, *a, ctypes.byref(n))
+        self._chk(call(None, None, None))
         ia = np.empty(n.value, dtype=np.int32)
         ja = np.empty(n.value, dtype=np.int32)
         a = np.empty(n.value, dtype=np.complex128)
-        self._chk(self.L.mvf_export_coo(self.h, f, _p(ia), _p(ja), _p(a), ctypes.byref(n)))
+        self._chk(call(_p(ia), _p(ja), _p(a)))
+        if drop_zeros:
+            self.zeros_dropped = z.value
         return ia, ja, a
 
     def export_rhs(self, f: int = 0):

@@ -30,11 +30,16 @@ def sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
 
 
+def host_sources():
+    """Host-only translation units (g++, no floating-point contraction)."""
+    return sorted(glob.glob(os.path.join(CSRC, "*.cpp")))
+
+
 def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + [
+    deps = sources() + host_sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + [
         os.path.join(HERE, "..", "include", "movfem_gpu.h"), __file__]
     return any(os.path.getmtime(d) > t for d in deps)
 
@@ -48,18 +53,23 @@ def build(force: bool = False, verbose: bool = False) -> str:
                     "-DNDEBUG"]
     objs = []
 
+    host_flags = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-DNDEBUG"]
+
     def one(src):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + f".{os.getpid()}.o")
-        cmd = [cc, *flags, "-c", src, "-o", obj]
+        obj = os.path.join(BUILD, os.path.basename(src).rsplit(".", 1)[0] + f".{os.getpid()}.o")
+        if src.endswith(".cpp"):
+            cmd = [shutil.which("g++") or "g++", *host_flags, "-c", src, "-o", obj]
+        else:
+            cmd = [cc, *flags, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stderr}")
+            raise RuntimeError(f"compile failed on {os.path.basename(src)}:\n{r.stderr}")
         if verbose and r.stderr:
             print(r.stderr)
         return obj
 
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(one, sources()))
+        objs = list(ex.map(one, sources() + host_sources()))
     tmp = LIB + f".{os.getpid()}.tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fopenmp", "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

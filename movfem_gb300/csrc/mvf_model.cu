@@ -520,4 +520,5 @@ extern "C" int mvf_map_model(const mvf_mesh *grid, const mvf_model *md, double o
 
 namespace mvf {
 const char *map_last_error() { return g_map_err.c_str(); }
+void set_host_error(const char *msg) { g_map_err = msg; }
 }  // namespace mvf

@@ -1583,17 +1583,24 @@ extern "C" int mvf_export_rhs(const mvf_ctx *xc, int32_t f, double *rhs) {
     return 0;
 }
 
-extern "C" int mvf_export_coo(const mvf_ctx *xc, int32_t f, int32_t *ia, int32_t *ja, double *a, int64_t *nnz) {
-    if (!xc || !nnz) return MVF_E_ARG;
-    Ctx *c = const_cast<Ctx *>(&xc->c);
+// Lower-triangle COO of frequency f in row-major order (global_vfem's arrays before
+// ga_sort_sparse).  drop: leave out the entries whose complex value is exactly zero and
+// count them, as find_zeros / rem_zeros do before the MUMPS call
+// (global_assembly.f90:123-150, MoVFEM_3DMT.f90:85-97); -0.0 counts as zero there too.
+static int export_coo(Ctx *c, int32_t f, int32_t *ia, int32_t *ja, double *a, int64_t *nnz, int64_t *nzero,
+                      bool drop) {
     if (!c->assembled) return fail(c, MVF_E_STATE, "assemble first");
     if (f < 0 || f >= c->nfreq) return fail(c, MVF_E_ARG, "bad frequency");
-    *nnz = c->nnz_lower;
-    if (!ia && !ja && !a) return 0;
-    if (!ia || !ja || !a) return fail(c, MVF_E_ARG, "ia, ja and a must all be given");
+    const bool want = ia || ja || a;
+    if (want && (!ia || !ja || !a)) return fail(c, MVF_E_ARG, "ia, ja and a must all be given");
+    if (!drop && !want) {
+        *nnz = c->nnz_lower;
+        return 0;
+    }
     const MatrixSet *S = nullptr;
     for (const MatrixSet &s : c->sets)
         if (f >= s.first_freq && f < s.first_freq + s.nfreq) S = &s;
+    if (!S) return fail(c, MVF_E_STATE, "no matrix set holds this frequency");
     std::vector<int64_t> rp(c->nne + 1);
     std::vector<int32_t> cl(c->nnz);
     std::vector<double> K(c->nnz), M(c->nnz);
@@ -1602,15 +1609,35 @@ extern "C" int mvf_export_coo(const mvf_ctx *xc, int32_t f, int32_t *ia, int32_t
     MVF_CUDA(c, cudaMemcpy(K.data(), S->K64, K.size() * sizeof(double), cudaMemcpyDeviceToHost));
     MVF_CUDA(c, cudaMemcpy(M.data(), S->M64, M.size() * sizeof(double), cudaMemcpyDeviceToHost));
     const double w32 = (c->mesh.quirks & MVF_Q_FP32_CONST) ? (double)(float)c->omega[f] : c->omega[f];
-    int64_t q = 0;
+    int64_t q = 0, zeros = 0;
     for (int32_t r = 0; r < c->nne; ++r)
         for (int64_t k = rp[r]; k < rp[r + 1]; ++k) {
             if (cl[k] > r) continue;
-            ia[q] = r + 1;
-            ja[q] = cl[k] + 1;
-            a[2 * q] = K[k];
-            a[2 * q + 1] = w32 * M[k];
+            const double re = K[k], im = w32 * M[k];
+            if (drop && re == 0.0 && im == 0.0) {
+                ++zeros;
+                continue;
+            }
+            if (want) {
+                ia[q] = r + 1;
+                ja[q] = cl[k] + 1;
+                a[2 * q] = re;
+                a[2 * q + 1] = im;
+            }
             ++q;
         }
+    *nnz = q;
+    if (nzero) *nzero = zeros;
     return 0;
+}
+
+extern "C" int mvf_export_coo(const mvf_ctx *xc, int32_t f, int32_t *ia, int32_t *ja, double *a, int64_t *nnz) {
+    if (!xc || !nnz) return MVF_E_ARG;
+    return export_coo(const_cast<Ctx *>(&xc->c), f, ia, ja, a, nnz, nullptr, false);
+}
+
+extern "C" int mvf_export_coo_nz(const mvf_ctx *xc, int32_t f, int32_t *ia, int32_t *ja, double *a, int64_t *nnz,
+                                 int64_t *nzero) {
+    if (!xc || !nnz || !nzero) return MVF_E_ARG;
+    return export_coo(const_cast<Ctx *>(&xc->c), f, ia, ja, a, nnz, nzero, true);
 }

@@ -221,6 +221,18 @@ def synthetic_geomodel(seed: int, mesh: "Mesh", *, spacing: float, depth: float,
     return GeoModel(xm=xm, ym=ym, zm=zm, sigma=sigma, ijsigma=ijs, mu=mu, ijmu=ijm)
 
 
+def from_grid(info: dict, xp: np.ndarray, yp: np.ndarray, zp: np.ndarray, **kw) -> Mesh:
+    """The mesh of a grid built by :func:`movfem_gb300.api.grid_3d` (grid_3d's node
+    coordinates, padding and layer counts), before the model mapping fills its nodal
+    conductivity and permeability (zero here; :func:`movfem_gb300.api.map_model` gives
+    them).  Keyword arguments set the boundary fields (dirichlet, gpml_sch, ...)."""
+    npt = int(info["npt"])
+    return Mesh(nodes_per_elem=int(info["nodes_per_elem"]), nx=int(info["nx"]), ny=int(info["ny"]),
+                nz=int(info["nz"]), xp=xp, yp=yp, zp=zp, sigma=np.zeros((npt, 6), dtype=np.complex128),
+                mu=np.zeros((npt, 6)), nextd=int(info["nextd"]), nzl_top=int(info["nzl_top"]),
+                nzl_air=int(info["nzl_air"]), ztop=float(info["ztop"]), **kw)
+
+
 def _padding(n: int, d: float) -> np.ndarray:
     return np.array([GROWTH * i * d for i in range(1, n + 1)])
 

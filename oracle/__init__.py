@@ -117,6 +117,15 @@ def map_model(mesh, model, omega):
     return sigma, mu
 
 
+def rem_zeros(ia, ja, a):
+    """find_zeros + rem_zeros (global_assembly.f90:123-150) as the driver applies them
+    before the MUMPS call (MoVFEM_3DMT.f90:85-97): the entries whose complex value equals
+    0 + 0i (so -0.0 too) are left out, the others keep their order.  Returns
+    (ia, ja, a, number dropped)."""
+    keep = a != 0
+    return ia[keep], ja[keep], a[keep], int(a.size - keep.sum())
+
+
 class Oracle:
     """Oracle bound to one mesh (keeps the numpy buffers alive)."""
 

@@ -60,12 +60,23 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("mn", ORDERS)
-@pytest.mark.parametrize("kind", ["dirichlet", "dirichlet-aniso", "topo", "gpml-fang", "gpml-zhou"])
+@pytest.mark.parametrize("kind", ["dirichlet", "dirichlet-aniso", "topo", "gpml-fang", "gpml-zhou", "mu-tensor"])
 def test_element_matrices(mn, kind):
     if kind == "topo":
         m = models.topo(mn)
     elif kind.startswith("gpml"):
         m = models.box(mn, n=(3, 3, 2), dirichlet=0, nextd=1, gpml_sch=0 if kind.endswith("fang") else 1, seed=3)
+    elif kind == "mu-tensor":
+        # mu != mu0: a full SPD permeability tensor per node exercises mu^-1 in the
+        # curl-curl integrand and the curl source of the primary H field
+        # (problem.f90:376-457, pe_modelcurl / pe_dmodel_pfield)
+        m = models.box(mn, seed=9)
+        rng = np.random.Generator(np.random.PCG64(12))
+        mu0 = 4e-7 * math.pi
+        rel = np.zeros((m.npt, 6))
+        rel[:, [0, 3, 5]] = 1.0 + rng.uniform(0.0, 0.5, (m.npt, 3))
+        rel[:, [1, 2, 4]] = rng.uniform(-0.05, 0.05, (m.npt, 3))
+        m.mu = rel * mu0
     else:
         m = models.box(mn, aniso=kind.endswith("aniso"), seed=4)
     w = 2 * math.pi * np.array([0.5, 3.0])
@@ -100,6 +111,32 @@ def test_assembled_system(mn, dirichlet):
         assert np.array_equal(ia, ria[low][order]) and np.array_equal(ja, rja[low][order])
         assert _rel(a, ref) < 1e-10
         assert _rel(p.export_rhs(f), rrhs) < 1e-10
+
+
+@pytest.mark.parametrize("mn", ORDERS)
+def test_zero_drop(mn):
+    """The export with exact zeros left out (find_zeros / rem_zeros) keeps the order of
+    the full export and drops exactly its 0 + 0i entries; against the oracle's dropped set
+    the two may differ only on entries that are cancellation noise (|a| <= 1e-14 max|a|),
+    which two summation orders can round to zero or not."""
+    m = models.box(mn, n=(3, 3, 2), seed=5)
+    w = 2 * math.pi * 0.5
+    p = _problem(m)
+    p.assemble([w])
+    ia, ja, a = p.export_coo(0)
+    ka, kb, kv = p.export_coo(0, drop_zeros=True)
+    zero = a == 0
+    assert p.zeros_dropped == int(zero.sum()) and kv.size + p.zeros_dropped == a.size
+    assert np.array_equal(ka, ia[~zero]) and np.array_equal(kb, ja[~zero]) and np.array_equal(kv, a[~zero])
+    o = oracle.Oracle(m)
+    ra, _ = o.assemble(w)
+    ria, rja = o.coo_coords()
+    low = ria >= rja
+    order = np.lexsort((rja[low], ria[low]))
+    ref = ra[low][order]
+    _, _, _, nref = oracle.rem_zeros(ria[low][order], rja[low][order], ref)
+    differ = zero != (ref == 0)
+    assert np.all(np.abs(np.where(zero, ref, a)[differ]) <= 1e-14 * np.abs(ref).max())
 
 
 @pytest.mark.parametrize("mn", ORDERS)

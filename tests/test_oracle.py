@@ -123,3 +123,15 @@ def test_golden_fixtures():
             assert np.array_equal(g[k], cur[k]), k
         else:
             assert np.allclose(g[k], cur[k], rtol=1e-12, atol=1e-300), k
+
+
+def test_rem_zeros_drops_exact_zeros_only():
+    """find_zeros / rem_zeros (global_assembly.f90:123-150): 0 + 0i and -0.0 are dropped,
+    tiny and purely imaginary values are kept, the order of the rest is unchanged."""
+    a = np.array([1 + 1j, 0j, complex(-0.0, 0.0), 1e-300 + 0j, 0 + 2j, complex(0.0, -0.0), 3 + 0j])
+    ia = np.arange(1, 8, dtype=np.int32)
+    ja = ia[::-1].copy()
+    ka, kb, kv, n = oracle.rem_zeros(ia, ja, a)
+    assert n == 3
+    assert list(ka) == [1, 4, 5, 7] and list(kb) == [7, 4, 3, 1]
+    assert np.array_equal(kv, a[[0, 3, 4, 6]])
