@@ -57,6 +57,30 @@ def test_noalloc_spmv_matches_spmv_twice():
         assert _rel(y, ref_oracle) < 1e-10, f"call {call}"
 
 
+def test_noalloc_after_a_side_stream_event():
+    """The documented stream contract: x written on the caller's own (non-default)
+    stream, that stream's event waited for on the host -- no device-wide synchronise --
+    then the call; y is complete when the call returns."""
+    torch = pytest.importorskip("torch")
+    m = M.plain_linear_block(ncells=6, d=250.0, n_air=3, dz_air=500.0, nrx=2)
+    w = 2 * math.pi * 2.0
+    p = api.MTProblem(m, device=0)
+    p.assemble([w])
+    rng = np.random.Generator(np.random.PCG64(13))
+    x = rng.normal(size=(2, p.nne)) + 1j * rng.normal(size=(2, p.nne))
+    ref = p.spmv(0, x)
+    side = torch.cuda.Stream(device=0)
+    with torch.cuda.stream(side):
+        xh = torch.from_numpy(x).pin_memory()
+        xd = xh.to("cuda:0", non_blocking=True)
+        yd = torch.zeros((2, p.nne), dtype=torch.complex128, device="cuda:0")
+        done = torch.cuda.Event()
+        done.record(side)
+    done.synchronize()
+    p.spmv_noalloc(0, xd.data_ptr(), yd.data_ptr())
+    assert _rel(yd.cpu().numpy(), ref) < 1e-12
+
+
 def test_noalloc_rejects_models_above_its_limit():
     torch = pytest.importorskip("torch")
     # 46^3 earth cells + 10 air layers: about 355,000 free DOFs, above the 262,144 limit
