@@ -73,6 +73,41 @@ def test_native_matches_oracle(mn, n_if):
 
 # (frequency, conductivity, nd): ddx/depth >= 2.5; in [1.5, 2.5), where the reference
 # leaves nd unset; <= 1/1.5; in (1/1.5, 1.5)
+def _strip(n, width, seed):
+    """n interface points in a narrow strip about y = 300: nearly collinear, so QSHEP2
+    needs more equations (its label 7 path), the capped radius (label 9) and, for the
+    narrowest, the damped linear fit (label 10)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x = rng.uniform(-100, 700, n)
+    return np.stack([x, 300 + rng.uniform(-width, width, n), 20 * np.sin(x / 150)], 1)
+
+
+def _regular(n):
+    """n x n points on a regular grid: equal distances everywhere (GETNP2's ties)."""
+    gx, gy = np.meshgrid(np.linspace(-100, 700, n), np.linspace(-100, 700, n), indexing="ij")
+    return np.stack([gx.ravel(), gy.ravel(), (40 * np.sin(gx / 200) * np.cos(gy / 170)).ravel()], 1)
+
+
+@pytest.mark.parametrize("surface", ["strip-10-0", "strip-20-4", "strip-21-0.5-1", "strip-25-0.2-7",
+                                     "strip-60-4-6", "regular-5", "regular-8"])
+def test_every_shepard_branch_bit_exact(surface):
+    """The native fit and the restatement agree bit for bit on inputs that take each
+    branch of QSHEP2 (tie skipping, extra equations, radius cap, damped fit)."""
+    kind, *a = surface.split("-")
+    if kind == "regular":
+        surf = _regular(int(a[0]))
+    elif len(a) == 2:
+        surf = _strip(30, float(a[0]), int(a[1]))
+    else:
+        surf = _strip(int(a[0]), float(a[1]), int(a[2]))
+    g = _case(20)
+    g.interfaces = [surf]
+    o = G.grid_3d(g)
+    info, xp, yp, zp, nzl = _native(g)
+    assert np.array_equal(nzl, o.nzl)
+    assert np.array_equal(xp, o.xp) and np.array_equal(yp, o.yp) and np.array_equal(zp, o.zp)
+
+
 @pytest.mark.parametrize("freq,sigma,nd", [(100.0, 1.0, 1.5), (1.0, 1.0, 2.0), (0.05, 0.01, 2.0), (0.4, 1.0, 3.0)])
 def test_padding_follows_the_skin_depth(freq, sigma, nd):
     """extension (geometry.f90:224-344): nextd is the first count >= 2 whose widths
