@@ -540,7 +540,7 @@ def run_reference(args):
         return
     if m.npt > 60000:
         print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable": (
-            "the reference (Fortran + MUMPS 4.10) cannot be built here or on the GPU box, and its stand-in (C "
+            "the reference (Fortran + MUMPS 4.10) cannot be built without a Fortran compiler, and its stand-in (C "
             "restatement + SuperLU direct solve) on this %d-DOF quadratic system would take hours and far more "
             "host memory than a bounded run allows (fill grows like n^(4/3), flops like n^2); the GPU arm's "
             "cpu_baseline gives a measured scaled sample and its labelled extrapolation" % full_dofs(m))}))

@@ -6,7 +6,7 @@ plus an FP64 direct solve with SciPy's SuperLU standing in for MUMPS 4.10 (the
 reference's third-party solver; it is not vendored and not installed here).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
-use this package, and only as the checker.  The product library never loads it.
+use this package, and only to compare against.  The product library never loads it.
 
 Parity pin: the reference (Fortran + MUMPS) cannot be compiled on either machine, so
 no reference outputs exist; "parity unpinned" against the reference itself.  The
@@ -118,7 +118,7 @@ def map_model(mesh, model, omega):
 
 
 def rem_zeros(ia, ja, a):
-    """find_zeros + rem_zeros (global_assembly.f90:123-150) as the driver applies them
+    """find_zeros + rem_zeros (global_assembly.f90:123-150) as MoVFEM_3DMT.f90 applies them
     before the MUMPS call (MoVFEM_3DMT.f90:85-97): the entries whose complex value equals
     0 + 0i (so -0.0 too) are left out, the others keep their order.  Returns
     (ia, ja, a, number dropped)."""

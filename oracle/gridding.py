@@ -3,8 +3,8 @@ the modified quadratic Shepard interpolation it calls (ACM TOMS algorithm 660, R
 1988: ``QSHEP2`` / ``QS2VAL`` with ``STORE2``, ``GETNP2``, ``SETUP2``, ``GIVENS``,
 ``ROTATE``; the reference carries a Fortran 90 version in toms660.f90).
 
-TEST INFRASTRUCTURE ONLY: the checker of ``movfem_gb300``'s native gridding
-(``mvf_grid_3d``).  Nothing in the product imports it.
+TEST INFRASTRUCTURE ONLY: the oracle the tests compare ``movfem_gb300``'s native
+gridding (``mvf_grid_3d``) against.  Nothing in the product imports it.
 
 The loops follow the Fortran statement by statement, 1-based (index 0 of every array is
 unused), so that each node is written in the same order and the last write wins as it
