@@ -85,6 +85,60 @@ def edge_factor(mn, i, d, t):
     return f.prod(1)
 
 
+def nodal_fn(mn, i, t):
+    """Shape function of node i (0-based) of the 20- or 27-node element at points t [n, 3]
+    (the serendipity and Lagrange families of n_fem.f90:138-317)."""
+    a = NR[:, i]
+    if mn == 20:
+        if i < 8:
+            p = np.prod([1 + a[k] * t[:, k] for k in range(3)], axis=0)
+            return p * (a[0] * t[:, 0] + a[1] * t[:, 1] + a[2] * t[:, 2] - 2) / 8
+        return 0.25 * np.prod([(1 - t[:, k] ** 2) if a[k] == 0 else (1 + a[k] * t[:, k]) for k in range(3)], axis=0)
+    return np.prod([(1 - t[:, k] ** 2) if a[k] == 0 else 0.5 * a[k] * t[:, k] * (1 + a[k] * t[:, k])
+                    for k in range(3)], axis=0)
+
+
+def grad_local(mn):
+    """[me, mn]: the gradient of node function n as a combination of the element's edge
+    functions, sum_i G[i, n] * edge fn i (exact: the edge space contains the gradients of
+    the nodal space; the coefficients are multiples of 1/8)."""
+    t = np.random.default_rng(1).uniform(-1, 1, (400, 3))
+    en, ed = EDGES[mn]
+    G = np.zeros((len(en), mn))
+    h = 1e-5
+    for n in range(mn):
+        for d in range(3):
+            tp, tm = t.copy(), t.copy()
+            tp[:, d] += h
+            tm[:, d] -= h
+            target = (nodal_fn(mn, n, tp) - nodal_fn(mn, n, tm)) / (2 * h)
+            idx = [i for i in range(len(en)) if ed[i] - 1 == d]
+            B = np.stack([edge_factor(mn, en[i] - 1, d, t) for i in idx], 1)
+            G[idx, n] = np.round(np.linalg.lstsq(B, target, rcond=None)[0] * 8) / 8
+    return G
+
+
+def node_ids(m):
+    """[mn, ne]: global grid node (i*nny + j)*nnz + k of every element's local nodes."""
+    o = m.nord - 1
+    ie, je, ke = [v.ravel() for v in np.meshgrid(np.arange(m.nx), np.arange(m.ny), np.arange(m.nz), indexing="ij")]
+    out = np.zeros((m.nodes_per_elem, ie.size), dtype=np.int64)
+    for l in range(m.nodes_per_elem):
+        a, b, c = NR[:, l] + 1
+        out[l] = ((o * ie + a) * m.nny + o * je + b) * m.nnz + o * ke + c
+    return out
+
+
+def discrete_gradient(m, gne, n):
+    """[n, npt] sparse: edge-DOF coefficients of the gradient of every grid node's
+    function (20/27-node meshes); nodes on the outer boundary are left out, since with
+    the Dirichlet boundary their gradients lose the boundary edges."""
+    G = _csr_from_local(grad_local(m.nodes_per_elem), gne, node_ids(m) + 1, n, m.npt)
+    i, j, k = np.meshgrid(np.arange(m.nnx), np.arange(m.nny), np.arange(m.nnz), indexing="ij")
+    inner = ((i > 0) & (i < m.nnx - 1) & (j > 0) & (j < m.nny - 1) & (k > 0) & (k < m.nnz - 1)).ravel()
+    return (G @ sp.diags(inner.astype(float))).tocsr()
+
+
 def p_local(mn):
     """[me, 12]: 12-edge basis function j = sum_i P[i, j] * (mn-node element's edge fn i)."""
     t = np.random.default_rng(0).uniform(-1, 1, (400, 3))
@@ -232,7 +286,7 @@ class Multilevel:
     """The preconditioner of one frequency w (angular; FP32-rounded as the assembly
     does when the mesh keeps the FP32-constant quirk) for mesh m (20/27 nodes)."""
 
-    def __init__(self, m, omega, floor=1e-8, tau=0.0, semidefinite=True):
+    def __init__(self, m, omega, floor=1e-8, tau=0.0, semidefinite=True, surface_gradient=False):
         from . import lib
         w = float(np.float32(omega)) if (m.quirks & 2) else float(omega)
         o = Oracle(m)
@@ -268,6 +322,29 @@ class Multilevel:
             cur, g, n = cm, gc, nc
         self.coarse = np.linalg.inv(self.A[-1].toarray())
         self.sizes = [a.shape[0] for a in self.A]
+        self.surface = None
+        if surface_gradient:
+            self.surface = self._surface_gradient(m, gq, nq)
+
+    def _surface_gradient(self, m, gq, nq):
+        """Gradient-space correction on the node layers around the earth's surface, with
+        the true operator.  Just above the surface the quadratic interpolation of the nodal
+        conductivity (earth value at the surface nodes, 0 above) dips below zero, to
+        -sigma/8 at mid-height of the first air cells, so the true A is indefinite on the
+        gradients there while the preconditioner's mass is positive: those modes are solved
+        exactly here, G_s (G_s^T A G_s)^-1 G_s^T, G_s the gradients of the grid nodes from
+        one node layer below the surface to the top of the first air cells."""
+        import scipy.sparse.linalg as spla
+        o = m.nord - 1
+        ksurf = o * (m.nz - m.nzl_air - m.nzl_top)
+        kk = np.arange(m.npt) % m.nnz
+        G = discrete_gradient(m, gq, nq)
+        cols = np.nonzero((kk >= ksurf - 1) & (kk <= ksurf + o))[0]
+        Gs = G[:, cols].tocsr()
+        used = np.nonzero(np.asarray(abs(Gs).sum(axis=0)).ravel() > 0)[0]
+        Gs = Gs[:, used].tocsr()
+        lu = spla.splu((Gs.T @ self.A_true @ Gs).tocsc())
+        return Gs, lu
 
     def _cycle(self, l, b):
         if l == len(self.A) - 1:
@@ -281,8 +358,15 @@ class Multilevel:
             x = x + Bc @ (b - A @ x)
         return x
 
+    def _apply(self, r):
+        z = self._cycle(0, r)
+        if self.surface is not None:
+            Gs, lu = self.surface
+            z = z + Gs @ lu.solve(Gs.T @ (r - self.A_true @ z))
+        return z
+
     def __call__(self, r):
         r = np.asarray(r, dtype=np.complex128)
         if r.ndim == 1:
-            return self._cycle(0, r)
-        return np.stack([self._cycle(0, r[:, q]) for q in range(r.shape[1])], 1)
+            return self._apply(r)
+        return np.stack([self._apply(r[:, q]) for q in range(r.shape[1])], 1)
