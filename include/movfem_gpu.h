@@ -172,6 +172,16 @@ int mvf_profile_mg(mvf_ctx *ctx, int32_t reps, double *sec_per_sweep, int64_t *b
  * sides (default), 1 solves one frequency (2 right-hand sides) per batch, so that each
  * frequency stops at its own iteration count. */
 int mvf_set_batching(mvf_ctx *ctx, int32_t per_frequency);
+/* Surface gradient correction of the multilevel preconditioner (36/54-DOF elements;
+ * no counterpart in the reference, which factorises): after each cycle the gradient
+ * modes of the grid nodes from one node layer below the earth's surface to the top of
+ * the first air cells are solved exactly with the true operator, where the quadratic
+ * interpolation of the nodal conductivity makes it indefinite.  The nodal system of
+ * those layers is factorised once per assembled matrix set (band LU on the host CPU)
+ * and solved on the host between two device stages of each application.  on = 1
+ * enables (MVF_E_UNSUPPORTED without the multilevel preconditioner, MVF_E_ARG when the
+ * grid has no surface between its earth and air layers), 0 disables. */
+int mvf_set_surface_correction(mvf_ctx *ctx, int32_t on);
 /* Arithmetic the last vertex-patch inversion set up: 0 no patches (12-DOF elements),
  * 1 FP64, 2 float-float (scaled inverses split into FP32 halves). */
 int32_t mvf_patch_arithmetic(const mvf_ctx *ctx);

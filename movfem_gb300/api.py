@@ -58,7 +58,7 @@ EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numb
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
            "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many", "mvf_profile_patch",
-           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model", "mvf_set_preconditioner", "mvf_mg_levels", "mvf_mg_apply_once", "mvf_profile_mg", "mvf_set_batching",
+           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model", "mvf_set_preconditioner", "mvf_mg_levels", "mvf_mg_apply_once", "mvf_profile_mg", "mvf_set_batching", "mvf_set_surface_correction",
            "mvf_grid_3d", "mvf_grid_get_info", "mvf_grid_export", "mvf_grid_destroy"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
                "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params", "mvf_patch_arithmetic",
@@ -119,6 +119,7 @@ def load(build: bool = True):
     L.mvf_mg_apply_once.argtypes = [P, I32, I32, P, P]
     L.mvf_profile_mg.argtypes = [P, I32, P, P]
     L.mvf_set_batching.argtypes = [P, I32]
+    L.mvf_set_surface_correction.argtypes = [P, I32]
     L.mvf_patch_arithmetic.argtypes = [P]
     L.mvf_patch_arithmetic.restype = I32
     L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
@@ -412,6 +413,11 @@ class MTProblem:
     def set_batching(self, per_frequency: bool):
         """Mixed mode: one batch per frequency (True) or all frequencies at once (False)."""
         self._chk(self.L.mvf_set_batching(self.h, int(per_frequency)))
+
+    def set_surface_correction(self, on: bool = True):
+        """After each multilevel cycle, solve the gradient modes of the layers around the
+        earth's surface exactly with the true operator (``mvf_set_surface_correction``)."""
+        self._chk(self.L.mvf_set_surface_correction(self.h, int(on)))
 
     def mg_levels(self):
         """Free DOFs of each level of the multilevel preconditioner (empty if unused)."""

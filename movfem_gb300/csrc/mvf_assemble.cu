@@ -1046,6 +1046,7 @@ extern "C" int mvf_assemble(mvf_ctx *x, int32_t nfreq, const double *omega, cons
         if (rc) return rc;
     }
     c->assembled = true;
+    ++c->asm_gen;
     return 0;
 }
 

@@ -197,6 +197,11 @@ struct Ctx {
     int mg_abs = 1;       // shift the preconditioner's conductivity positive semidefinite
     int freq_batch = 0;  // mixed mode: 0 every frequency of a matrix set in one batch, 1 one per batch
     std::vector<MgLevel> mg;
+    // surface gradient correction of the multilevel method (mvf_surface.cu) and the
+    // count of assemblies (its factors are cached per matrix set and assembly)
+    int surf_on = 0;
+    struct Surface *surf = nullptr;
+    uint64_t asm_gen = 0;
 };
 
 // process-wide count of the library's kernel launches.  While a thread captures a
@@ -258,6 +263,13 @@ void patch_apply(Ctx *c, const double2 *inv, int R, int npol, int nfi, const dou
 // multilevel preconditioner (mvf_mg.cu)
 int mg_setup(Ctx *c);          // hierarchy, once per context
 void mg_release(Ctx *c);
+// surface gradient correction (mvf_surface.cu)
+struct SurfJob;
+int surf_setup(Ctx *c);
+void surf_release(Ctx *c);
+int surf_numeric(Ctx *c, const MatrixSet &S, const double *wq, int R, SurfJob **out);
+void surf_apply(Ctx *c, SurfJob *J, const MatrixSet &S, const double *d_wq, const double2 *r, double2 *z, double2 *t);
+void surf_free(SurfJob *J);
 struct MgWork;                  // numeric state of one solve batch
 int mg_numeric(Ctx *c, const MatrixSet &S, const double *w, int nf, int R, int npol, MgWork **out);
 void mg_apply(Ctx *c, MgWork *W, const double2 *r, double2 *z);

@@ -699,6 +699,7 @@ struct MgWork {
     float2 *Kff = nullptr, *Mff = nullptr;  // level-0 K and Mp as FP32 halves
     float2 *wff = nullptr;                  // [R] angular frequencies as FP32 halves
     float4 *bff = nullptr, *xff = nullptr;  // level-0 right-hand side and iterate, [n][R]
+    SurfJob *sj = nullptr;                  // surface gradient correction after each cycle
 };
 
 // patch-inverse workspace rows of one level: blocks x pmax x 2 pmax complex
@@ -732,6 +733,8 @@ void mg_free(Ctx *c, MgWork *W) {
     p.push_back(W->xff);
     for (void *q : p)
         if (q) cudaFree(q);
+    surf_free(W->sj);
+    W->sj = nullptr;
     delete W;
 }
 
@@ -858,6 +861,12 @@ int mg_numeric(Ctx *c, const MatrixSet &S, const double *w, int nf, int R, int n
         mg_free(c, W);
         return fail(c, MVF_E_SINGULAR, "multilevel preconditioner: zero pivot or missing pattern entry");
     }
+    if (c->surf_on) {
+        if (int rc = surf_numeric(c, S, wq.data(), R, &W->sj)) {
+            mg_free(c, W);
+            return rc;
+        }
+    }
     *out = W;
     return 0;
 }
@@ -938,6 +947,7 @@ void mg_apply(Ctx *c, MgWork *W, const double2 *r, double2 *z) {
     vcycle(c, W, 0);
     W->b[0] = nullptr;
     W->x[0] = nullptr;
+    if (W->sj) surf_apply(c, W->sj, *W->S, W->wq, r, z, W->t[0]);
 }
 
 }  // namespace mvf

@@ -498,6 +498,7 @@ static int create(Ctx *c, const mvf_mesh *m, int device) {
 static void release(Ctx *c) {
     free_sets(c);
     mg_release(c);
+    surf_release(c);
     void *ptrs[] = {c->d.xp, c->d.yp, c->d.zp, c->d.sigma, c->d.sigma_f, c->d.mu, c->d.gne, c->d.elem_color,
                     c->d.N, c->d.dN, c->d.L, c->d.dL, c->d.gp, c->d.Gloc, c->d.edge_node, c->d.edge_dir,
                     c->d.rowptr, c->d.col, c->d.grow, c->d.gcol, c->d.gval, c->d.gtrow, c->d.gtcol, c->d.gtval,

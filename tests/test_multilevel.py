@@ -101,3 +101,50 @@ def test_per_frequency_batching_matches_joint_batch():
         Zs.append(p.impedance()[0])
     err = np.linalg.norm(Zs[0] - Zs[1], axis=2) / np.linalg.norm(Zs[1], axis=2)
     assert err.max() <= 1e-6
+
+
+@pytest.mark.parametrize("mn", [20, 27])
+def test_surface_correction_cycle_matches_cpu_reference(mn):
+    """The cycle followed by the surface gradient correction (mvf_surface.cu) against the
+    CPU restatement with ``surface_gradient=True`` (same slab, exact solve there)."""
+    f = 1.0
+    m = _model(mn, [f], dirichlet=1, ncx=4, ncz=3, nextd=1, n_air=2)
+    w = 2 * math.pi * f
+    ref = Multilevel(m, w, floor=1e-8, tau=0.0, semidefinite=True, surface_gradient=True)
+    p = api.MTProblem(m)
+    p.set_preconditioner(0, 1e-8, 0.0)
+    p.set_surface_correction(True)
+    p.assemble(np.array([w]), sigma_f=m.sigma_at(w)[None])
+    rng = np.random.Generator(np.random.PCG64(5))
+    r = rng.normal(size=(p.nne, 2)) + 1j * rng.normal(size=(p.nne, 2))
+    zg = p.mg_apply_once(0, r)
+    zr = ref(r)
+    assert np.linalg.norm(zg - zr) / np.linalg.norm(zr) < 1e-3
+
+
+@pytest.mark.parametrize("mode", [api.MODE_MIXED, api.MODE_FP64])
+def test_surface_correction_solve_matches_direct(mode):
+    """With the surface correction the quadratic Dirichlet solve reaches the FP64
+    tolerance in fewer iterations and still gives the direct solver's impedances."""
+    f = 1.0
+    m = _model(20, [f])
+    w = 2 * math.pi * f
+    o = oracle.Oracle(m)
+    o.set_sigma(m.sigma_at(w))
+    xd, A, rhs = o.solve_direct(w)
+    Zd = o.receivers(w, xd)[2]
+    iters = []
+    for on in (False, True):
+        p = api.MTProblem(m)
+        p.set_solver(restart=60)
+        p.set_surface_correction(on)
+        p.assemble(np.array([w]), sigma_f=m.sigma_at(w)[None])
+        x, st = p.solve(tol=1e-10, mode=mode, max_iters=600, raise_noconv=False)
+        iters.append(st["inner_iters"])
+        if on:
+            res = max(np.linalg.norm(rhs[k] - A @ x[0, k]) / np.linalg.norm(rhs[k]) for k in range(2))
+            assert res <= 1e-7, st
+            Z = p.impedance()[0][0]
+            err = np.linalg.norm(Z - Zd, axis=1) / np.linalg.norm(Zd, axis=1)
+            assert err.max() <= 1e-6, (err.max(), st)
+    assert iters[1] <= iters[0], iters
