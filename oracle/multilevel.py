@@ -324,11 +324,12 @@ class Multilevel:
         self.sizes = [a.shape[0] for a in self.A]
         self.surface = None
         if surface_gradient:
-            self.surface = self._surface_gradient(m, gq, nq)
+            self.surface = self._surface_gradient(m, gq, nq, surface_gradient == "negative")
 
-    def _surface_gradient(self, m, gq, nq):
-        """Gradient-space correction on the node layers around the earth's surface, with
-        the true operator.  Just above the surface the quadratic interpolation of the nodal
+    def _surface_gradient(self, m, gq, nq, negative=False):
+        """Gradient-space correction on the node layers around the earth's surface (and,
+        with ``negative``, on the nodes of every element whose interpolated conductivity
+        turns negative), with the true operator.  Just above the surface the quadratic interpolation of the nodal
         conductivity (earth value at the surface nodes, 0 above) dips below zero, to
         -sigma/8 at mid-height of the first air cells, so the true A is indefinite on the
         gradients there while the preconditioner's mass is positive: those modes are solved
@@ -339,7 +340,17 @@ class Multilevel:
         ksurf = o * (m.nz - m.nzl_air - m.nzl_top)
         kk = np.arange(m.npt) % m.nnz
         G = discrete_gradient(m, gq, nq)
-        cols = np.nonzero((kk >= ksurf - 1) & (kk <= ksurf + o))[0]
+        sel = (kk >= ksurf - 1) & (kk <= ksurf + o)
+        if negative:
+            # also the nodes of every element whose interpolated conductivity turns
+            # negative at one of its 27 Gauss points (block and layer edges inside the earth)
+            g = np.array([-math.sqrt(0.6), 0.0, math.sqrt(0.6)])
+            gp = np.array([[a, b, c] for a in g for b in g for c in g])
+            Nv = np.stack([nodal_fn(m.nodes_per_elem, i, gp) for i in range(m.nodes_per_elem)], 0)
+            ids = node_ids(m)
+            sg = Nv.T @ m.sigma[:, 0].real[ids]
+            sel[ids[:, sg.min(0) < 0].ravel()] = True
+        cols = np.nonzero(sel)[0]
         Gs = G[:, cols].tocsr()
         used = np.nonzero(np.asarray(abs(Gs).sum(axis=0)).ravel() > 0)[0]
         Gs = Gs[:, used].tocsr()
