@@ -182,6 +182,11 @@ int mvf_set_batching(mvf_ctx *ctx, int32_t per_frequency);
  * enables (MVF_E_UNSUPPORTED without the multilevel preconditioner, MVF_E_ARG when the
  * grid has no surface between its earth and air layers), 0 disables. */
 int mvf_set_surface_correction(mvf_ctx *ctx, int32_t on);
+/* Test hook (host only): the band LU with partial pivoting that the surface correction
+ * uses, on a dense column-major n x n matrix a (entries outside the band [-kl, ku]
+ * ignored), solving nrhs right-hand sides b [nrhs][n] in place.  MVF_E_SINGULAR on a
+ * zero pivot column. */
+int mvf_band_solve(int64_t n, int32_t kl, int32_t ku, const double *a, double *b, int32_t nrhs);
 /* Arithmetic the last vertex-patch inversion set up: 0 no patches (12-DOF elements),
  * 1 FP64, 2 float-float (scaled inverses split into FP32 halves). */
 int32_t mvf_patch_arithmetic(const mvf_ctx *ctx);

@@ -58,7 +58,7 @@ EXPORTS = ["mvf_create", "mvf_destroy", "mvf_last_error", "mvf_sizes", "mvf_numb
            "mvf_spmm_tuning", "mvf_spmm_variant", "mvf_set_guess", "mvf_net_create", "mvf_net_destroy",
            "mvf_net_last_error", "mvf_net_num_params", "mvf_net_get_params", "mvf_net_set_params", "mvf_net_forward",
            "mvf_net_gradients", "mvf_net_train_step", "mvf_node_fields", "mvf_solve_many", "mvf_profile_patch",
-           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model", "mvf_set_preconditioner", "mvf_mg_levels", "mvf_mg_apply_once", "mvf_profile_mg", "mvf_set_batching", "mvf_set_surface_correction",
+           "mvf_set_solver", "mvf_patch_arithmetic", "mvf_map_model", "mvf_set_preconditioner", "mvf_mg_levels", "mvf_mg_apply_once", "mvf_profile_mg", "mvf_set_batching", "mvf_set_surface_correction", "mvf_band_solve",
            "mvf_grid_3d", "mvf_grid_get_info", "mvf_grid_export", "mvf_grid_destroy"]
 _NOT_STATUS = ("mvf_destroy", "mvf_last_error", "mvf_create", "mvf_kernel_launches", "mvf_spmm_tuning",
                "mvf_net_destroy", "mvf_net_last_error", "mvf_net_num_params", "mvf_patch_arithmetic",
@@ -120,6 +120,7 @@ def load(build: bool = True):
     L.mvf_profile_mg.argtypes = [P, I32, P, P]
     L.mvf_set_batching.argtypes = [P, I32]
     L.mvf_set_surface_correction.argtypes = [P, I32]
+    L.mvf_band_solve.argtypes = [I64, I32, I32, P, P, I32]
     L.mvf_patch_arithmetic.argtypes = [P]
     L.mvf_patch_arithmetic.restype = I32
     L.mvf_net_create.argtypes = [ctypes.POINTER(P), I32, I32, I32, I32, P, ctypes.c_uint64, I32]
@@ -175,6 +176,19 @@ class GridInfo(ctypes.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def band_solve(a, b, kl: int, ku: int):
+    """Test hook: the surface correction's band LU (``mvf_band_solve``) on the band
+    [-kl, ku] of the dense matrix ``a`` [n, n], for ``b`` [n] or [n, nrhs]."""
+    L = load()
+    n = a.shape[0]
+    af = np.asfortranarray(a, dtype=np.float64)
+    bb = np.ascontiguousarray(np.asarray(b, dtype=np.float64).reshape(n, -1).T)
+    rc = L.mvf_band_solve(n, kl, ku, af.ctypes.data, bb.ctypes.data, bb.shape[0])
+    if rc != 0:
+        raise MVFError(rc, "band solve failed")
+    return bb.T.reshape(np.shape(b))
 
 
 def grid_3d(dx, dy, dz, high, depth, nodes_per_elem, sigma_bg, rx, interfaces, xm, ym, zm, freqs):

@@ -440,6 +440,21 @@ void surf_apply(Ctx *c, SurfJob *J, const MatrixSet &MS, const double *d_wq, con
 
 using namespace mvf;
 
+// Test hook (host only, no device): the band LU of the surface correction on a dense
+// column-major n x n matrix whose entries outside the band [-kl, ku] are ignored;
+// solves for nrhs right-hand sides b [nrhs][n] in place.
+extern "C" int mvf_band_solve(int64_t n, int32_t kl, int32_t ku, const double *a, double *b, int32_t nrhs) {
+    if (n < 1 || kl < 0 || ku < 0 || !a || !b || nrhs < 1) return MVF_E_ARG;
+    BandLU lu;
+    lu.init(n, kl, ku);
+    for (int64_t j = 0; j < n; ++j)
+        for (int64_t i = std::max<int64_t>(0, j - ku); i <= std::min<int64_t>(n - 1, j + kl); ++i)
+            lu.at(i, j) = a[(size_t)j * n + i];
+    if (!lu.factor()) return MVF_E_SINGULAR;
+    for (int32_t q = 0; q < nrhs; ++q) lu.solve(b + (size_t)q * n);
+    return 0;
+}
+
 extern "C" int mvf_set_surface_correction(mvf_ctx *xc, int32_t on) {
     if (!xc) return MVF_E_ARG;
     Ctx *c = &xc->c;

@@ -80,3 +80,23 @@ def test_surface_gradient_correction_removes_the_slow_tail():
     ml.surface = surface
     assert with_surface < 1e-8, with_surface
     assert plain > 1e-5, plain
+
+
+@pytest.mark.parametrize("n,kl,ku,pivot", [(50, 3, 3, False), (400, 17, 17, True), (300, 5, 40, True),
+                                            (1200, 90, 90, True)])
+def test_band_lu_of_the_surface_correction(n, kl, ku, pivot):
+    """The host band LU of mvf_surface.cu (partial pivoting, fill of kl extra rows)
+    against a dense solve; indefinite matrices with small diagonals force row swaps."""
+    from movfem_gb300 import api
+    rng = np.random.Generator(np.random.PCG64(n + kl))
+    a = rng.normal(size=(n, n))
+    i, j = np.indices((n, n))
+    a[(i - j > kl) | (j - i > ku)] = 0.0
+    if not pivot:
+        a[np.diag_indices(n)] += 2.0 * (kl + ku + 1)
+    else:
+        a[np.diag_indices(n)] *= 1e-3
+    b = rng.normal(size=(n, 3))
+    x = api.band_solve(a, b, kl, ku)
+    ref = np.linalg.solve(a, b)
+    assert np.abs(x - ref).max() <= 1e-8 * np.abs(ref).max()
